@@ -1,0 +1,210 @@
+/*
+ * lbgb300.h -- C ABI of the GB300 lattice Boltzmann library (liblbgb300.so).
+ *
+ * Part 1 are the reference's own entry points, with the reference's names,
+ * argument order and meaning, so that the reference's host loop
+ * (SimulationD2Q9/SimulationD3Q19::runLBM) links against this library
+ * unchanged.  Each declaration names the reference interface it replaces.
+ * Like the reference they return void; a failure is recorded and can be read
+ * with lb_abi_last_error().  grid/block are accepted for signature
+ * compatibility; the library picks its own launch shapes (and therefore does
+ * not require width % 32 == 0 or height % 4 == 0).
+ *
+ * Part 2 is this library's own context API: one lattice per context, state
+ * owned and laid out by the library, every call returns an lb_status.
+ */
+#ifndef LBGB300_H
+#define LBGB300_H
+
+#include <stdint.h>
+#include "lattibol.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ======================================================================== */
+/* Part 1: drop-in entry points                                             */
+/* ======================================================================== */
+
+/* replaces streaming_d2q9, reference src/streaming.h:31-32 */
+void streaming_d2q9(DataD2Q9 *data, dim3 grid, dim3 block);
+/* replaces streaming_d3q19, reference src/streaming.h:34-35 */
+void streaming_d3q19(DataD3Q19 *data, dim3 grid, dim3 block);
+
+/* replaces collision_d2q9, reference src/collision.h:27-31 (includes the
+ * Shan-Chen force step, reference src/collision.cu:352-354, when G < 0) */
+void collision_d2q9(float *plot_data, DataD2Q9 *data, float w0, float w1, float w5,
+                    float tau_inv, float ux_in, float uy_in, float rho_out, float u_min,
+                    float u_max, float rho_min, float rho_max, dim3 grid, dim3 block,
+                    float Fx, float Fy, float G, float Gads);
+/* replaces collision_d3q19, reference src/collision.h:33-36 */
+void collision_d3q19(float *plot_data, DataD3Q19 *data, float w0, float w1, float w7,
+                     float tau_inv, float ux_in, float uy_in, float uz_in, float rho_out,
+                     float u_min, float u_max, float rho_min, float rho_max, dim3 grid,
+                     dim3 block);
+
+/* replace get_border_d2q9/_d3q19, reference src/get_border.h:29-33 */
+void get_border_d2q9(DataD2Q9 *data, dim3 grid, dim3 block);
+void get_border_d3q19(DataD3Q19 *data, dim3 grid, dim3 block);
+/* replace apply_border_d2q9/_d3q19, reference src/apply_border.h:25-29 */
+void apply_border_d2q9(DataD2Q9 *data, dim3 grid, dim3 block);
+void apply_border_d3q19(DataD3Q19 *data, dim3 grid, dim3 block);
+
+/* replace read_value_2d/_3d, reference src/read_value.h:27-31.  plot_data may
+ * be NULL (headless), then the probe reads the moment arrays instead. */
+void read_value_2d(float *plot_data, DataD2Q9 *data, int x, int y, int z);
+void read_value_3d(float *plot_data, DataD3Q19 *data, int x, int y, int z);
+
+/* replaces copy_border_devices_d2q9, reference src/copy_border.h:30-35
+ * (extern "C" there; the stream is passed by reference in C++) */
+#ifdef __cplusplus
+void copy_border_devices_d2q9(float *nb_border_f1, float *nb_border_f5, float *nb_border_f8,
+                              float *nb_border_f3, float *nb_border_f6, float *nb_border_f7,
+                              float *border_f1, float *border_f5, float *border_f8,
+                              float *border_f3, float *border_f6, float *border_f7,
+                              int height, cudaStream_t &s);
+#else
+void copy_border_devices_d2q9(float *nb_border_f1, float *nb_border_f5, float *nb_border_f8,
+                              float *nb_border_f3, float *nb_border_f6, float *nb_border_f7,
+                              float *border_f1, float *border_f5, float *border_f8,
+                              float *border_f3, float *border_f6, float *border_f7,
+                              int height, cudaStream_t *s);
+#endif
+/* C-linkage twin of copy_border_devices_d3q19, which the reference declares
+ * with C++ linkage (reference src/copy_border.h:37-47); the library also
+ * exports that C++ symbol itself.  dst[10]/src[10] are in the order
+ * {f1, f7, f8, f9, f10, f2, f11, f12, f13, f14}. */
+void lb_copy_border_devices_d3q19(float *const dst[10], float *const src[10], int height,
+                                  int depth, cudaStream_t s);
+
+/* --- drop-in controls (no counterpart in the reference) ------------------ */
+#define LB_ABI_STANDALONE 0 /* streaming_* swaps in place, collision_* collides: the
+                               reference's two-pass scheme, bit-identical results */
+#define LB_ABI_FUSED 1      /* streaming_* records the step, collision_* runs one fused
+                               pull-stream+collide into a library-owned second population
+                               set and swaps the f* pointers inside *data */
+int lb_abi_set_mode(int mode);
+int lb_abi_get_mode(void);
+/* fused mode: copy the current populations back into the caller's original
+ * buffers, restore the caller's pointers in *data and free the second set */
+int lb_abi_release_d2q9(DataD2Q9 *data);
+int lb_abi_release_d3q19(DataD3Q19 *data);
+/* global conservation sums over non-solid nodes, accumulated in FP64 on the
+ * GPU from the moment arrays: out = {mass, mom_x, mom_y, mom_z, kinetic
+ * energy, max|u|, n_fluid}.  Blocks the calling thread until done. */
+int lb_reduce_d2q9(const DataD2Q9 *data, double out[7]);
+int lb_reduce_d3q19(const DataD3Q19 *data, double out[7]);
+/* last error recorded by a void drop-in call on this thread ("" if none) */
+const char *lb_abi_last_error(void);
+int lb_abi_clear_error(void);
+
+/* ======================================================================== */
+/* Part 2: context API                                                      */
+/* ======================================================================== */
+
+typedef enum {
+    LB_OK = 0,
+    LB_ERR_ARG = -1,     /* invalid argument or configuration */
+    LB_ERR_CUDA = -2,    /* a CUDA call failed (message in lb_error) */
+    LB_ERR_STATE = -3,   /* call not valid in the context's current state */
+    LB_ERR_NOMEM = -4,   /* device allocation failed */
+    LB_ERR_DEVICE = -5,  /* a kernel reported a device-side error (NaN census, bounds) */
+} lb_status;
+
+#define LB_D2Q9 9
+#define LB_D3Q19 19
+
+#define LB_MODE_REFERENCE 0 /* reference semantics: walls stored as full-way bounce-back,
+                               Zou-He inlet (x=0) and outlet (x=nx-1) always on */
+#define LB_MODE_NATIVE 1    /* periodic box, half-way bounce-back at wall cells,
+                               moving walls, body force, optional Shan-Chen */
+
+#define LB_STORE_F32 0
+#define LB_STORE_F16 1  /* populations stored as binary16 deviations f_k - w_k */
+#define LB_STORE_BF16 2 /* populations stored as bfloat16 deviations f_k - w_k */
+
+#define LB_PSI_REF 0    /* psi = 4 exp(-200/rho), the reference's form */
+#define LB_PSI_EXP1 1   /* psi = 1 - exp(-rho) */
+
+/* cell flags (lb_set_flags); in LB_MODE_REFERENCE any non-zero value is a
+ * solid node */
+#define LB_CELL_FLUID 0x00u
+#define LB_CELL_WALL 0x01u
+#define LB_CELL_MOVING 0x02u /* with LB_CELL_WALL: wall moving with config.wall_u */
+
+typedef struct {
+    int lattice;        /* LB_D2Q9 or LB_D3Q19 */
+    int nx, ny, nz;     /* nodes; nz = 1 for D2Q9 */
+    int mode;           /* LB_MODE_* */
+    int storage;        /* LB_STORE_* */
+    float tau_inv;      /* 1/tau */
+    float force[3];     /* body force (velocity-shift forcing) */
+    float u_in[3];      /* reference mode: inlet velocity (x used) */
+    float rho_out;      /* reference mode: outlet density */
+    float wall_u[3];    /* native mode: velocity of LB_CELL_MOVING walls */
+    float G, G_ads;     /* Shan-Chen interaction and adhesion strengths (0 = off) */
+    int psi_form;       /* LB_PSI_* */
+    int graph_steps;    /* steps per captured CUDA graph in lb_step (0 = default 64) */
+} lb_config;
+
+typedef struct lb_ctx lb_ctx;
+
+int lb_config_default(lb_config *cfg, int lattice, int nx, int ny, int nz);
+int lb_create(const lb_config *cfg, lb_ctx **out);
+int lb_destroy(lb_ctx *ctx);
+const char *lb_error(const lb_ctx *ctx);
+
+/* cell flags, one byte per node, host memory */
+int lb_set_flags(lb_ctx *ctx, const uint8_t *flags);
+/* populations in the library's SoA order f[k*N + node], host float memory */
+int lb_set_populations(lb_ctx *ctx, const float *f);
+int lb_get_populations(lb_ctx *ctx, float *f);
+/* equilibrium from host moment fields (any of ux/uy/uz may be NULL = 0; rho
+ * NULL = 1) */
+int lb_init_equilibrium(lb_ctx *ctx, const float *rho, const float *ux, const float *uy,
+                        const float *uz);
+/* advance nsteps time steps (asynchronous on the context's stream); the
+ * moments of the last step are written to the moment fields */
+int lb_step(lb_ctx *ctx, int nsteps);
+/* the moment fields of the last step (host memory; uz ignored for D2Q9) */
+int lb_get_moments(lb_ctx *ctx, float *rho, float *ux, float *uy, float *uz);
+/* conservation sums of the last step's moments, FP64 (see lb_reduce_d3q19) */
+int lb_reduce(lb_ctx *ctx, double out[7]);
+int lb_synchronize(lb_ctx *ctx);
+/* run nsteps and return the device time between CUDA events recorded on the
+ * context's stream (warm-up is the caller's business) */
+int lb_time_steps(lb_ctx *ctx, int nsteps, float *ms);
+/* number of kernel launches issued by this context so far */
+int64_t lb_launch_count(const lb_ctx *ctx);
+/* the moving-wall momentum term 6 w_k (c_k . wall_u) per direction, as used
+ * by the kernels (q = 9 or 19 floats) */
+int lb_wall_correction(const lb_ctx *ctx, float *corr);
+
+/* ---- device helpers (tests and hosts without their own allocator) ------ */
+int lb_device_count(int *n);
+int lb_malloc(void **ptr, size_t bytes);
+int lb_free(void *ptr);
+int lb_memcpy_h2d(void *dst, const void *src, size_t bytes);
+int lb_memcpy_d2h(void *dst, const void *src, size_t bytes);
+int lb_memset(void *dst, int value, size_t bytes);
+int lb_device_synchronize(void);
+const char *lb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+/* the reference's C++-linkage entry point, reference src/copy_border.h:37-47 */
+void copy_border_devices_d3q19(float *nb_border_f1, float *nb_border_f7, float *nb_border_f8,
+                               float *nb_border_f9, float *nb_border_f10, float *nb_border_f2,
+                               float *nb_border_f11, float *nb_border_f12,
+                               float *nb_border_f13, float *nb_border_f14, float *border_f1,
+                               float *border_f7, float *border_f8, float *border_f9,
+                               float *border_f10, float *border_f2, float *border_f11,
+                               float *border_f12, float *border_f13, float *border_f14,
+                               int height, int depth, cudaStream_t &s);
+#endif
+
+#endif

@@ -1,0 +1,17 @@
+"""GB300-native lattice Boltzmann hot path of lattibol.
+
+The compute lives in liblbgb300.so (hand-written CUDA for sm_103a behind a C
+ABI, see include/lbgb300.h).  This package only loads it and mirrors the
+reference's host-side interface for Python callers; it has no CPU fallback.
+"""
+from . import abi  # noqa: F401
+
+_lib = None
+
+
+def lib():
+    """The loaded liblbgb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        _lib = abi.load()
+    return _lib
