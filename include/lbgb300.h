@@ -95,6 +95,20 @@ int lb_abi_release_d3q19(DataD3Q19 *data);
  * energy, max|u|, n_fluid}.  Blocks the calling thread until done. */
 int lb_reduce_d2q9(const DataD2Q9 *data, double out[7]);
 int lb_reduce_d3q19(const DataD3Q19 *data, double out[7]);
+/* The reference's per-step host sequence (SimulationD3Q19::runLBM, reference
+ * src/simulation_d3q19.cu:350-430, without the GL map/unmap and the extra
+ * device-wide synchronisations): for each step streaming_d3q19,
+ * collision_d3q19 into plot_data, read_value_3d at the cursor and a 16-byte
+ * device-to-host copy of data->valueCur into value_host[4] (the value of the
+ * last step is left there).  Returns LB_OK or LB_ERR_CUDA (message in
+ * lb_abi_last_error). */
+typedef struct {
+    float w0, w1, w7, tau_inv, ux_in, uy_in, uz_in, rho_out;
+    int cursor[3];
+} lb_run_params_d3q19;
+int lb_run_lbm_d3q19(DataD3Q19 *data, float *plot_data, const lb_run_params_d3q19 *p, int steps,
+                     float *value_host);
+
 /* last error recorded by a void drop-in call on this thread ("" if none) */
 const char *lb_abi_last_error(void);
 int lb_abi_clear_error(void);
@@ -185,6 +199,8 @@ int lb_wall_correction(const lb_ctx *ctx, float *corr);
 int lb_device_count(int *n);
 int lb_malloc(void **ptr, size_t bytes);
 int lb_free(void *ptr);
+int lb_malloc_host(void **ptr, size_t bytes); /* page-locked host memory */
+int lb_free_host(void *ptr);
 int lb_memcpy_h2d(void *dst, const void *src, size_t bytes);
 int lb_memcpy_d2h(void *dst, const void *src, size_t bytes);
 int lb_memset(void *dst, int value, size_t bytes);

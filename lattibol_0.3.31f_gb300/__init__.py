@@ -15,3 +15,6 @@ def lib():
     if _lib is None:
         _lib = abi.load()
     return _lib
+
+
+from .lattice import DeviceData, Lattice, LBError, W2, W3  # noqa: E402,F401

@@ -67,6 +67,11 @@ class lb_config(ctypes.Structure):
                 ("psi_form", ctypes.c_int), ("graph_steps", ctypes.c_int)]
 
 
+class lb_run_params_d3q19(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("w0", "w1", "w7", "tau_inv", "ux_in", "uy_in",
+                                              "uz_in", "rho_out")] + [("cursor", ctypes.c_int * 3)]
+
+
 # constants of lbgb300.h
 LB_OK, LB_ERR_ARG, LB_ERR_CUDA, LB_ERR_STATE, LB_ERR_NOMEM, LB_ERR_DEVICE = 0, -1, -2, -3, -4, -5
 LB_D2Q9, LB_D3Q19 = 9, 19
@@ -100,6 +105,8 @@ PROTOTYPES = [
     ("lb_abi_release_d3q19", _c.c_int, [_c.POINTER(DataD3Q19)]),
     ("lb_reduce_d2q9", _c.c_int, [_c.POINTER(DataD2Q9), _c.POINTER(_c.c_double)]),
     ("lb_reduce_d3q19", _c.c_int, [_c.POINTER(DataD3Q19), _c.POINTER(_c.c_double)]),
+    ("lb_run_lbm_d3q19", _c.c_int, [_c.POINTER(DataD3Q19), _c.c_void_p,
+                                    _c.POINTER(lb_run_params_d3q19), _c.c_int, _c.c_void_p]),
     ("lb_abi_last_error", _c.c_char_p, []),
     ("lb_abi_clear_error", _c.c_int, []),
     ("lb_config_default", _c.c_int, [_c.POINTER(lb_config), _c.c_int, _c.c_int, _c.c_int,
@@ -121,6 +128,8 @@ PROTOTYPES = [
     ("lb_device_count", _c.c_int, [_c.POINTER(_c.c_int)]),
     ("lb_malloc", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
     ("lb_free", _c.c_int, [_c.c_void_p]),
+    ("lb_malloc_host", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
+    ("lb_free_host", _c.c_int, [_c.c_void_p]),
     ("lb_memcpy_h2d", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_size_t]),
     ("lb_memcpy_d2h", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_size_t]),
     ("lb_memset", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_size_t]),

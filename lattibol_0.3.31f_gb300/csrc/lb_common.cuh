@@ -1,0 +1,207 @@
+// lb_common.cuh -- lattice tables, pointer bundles and the per-node math that
+// every lattice Boltzmann kernel of the library shares.
+//
+// The library is compiled with -fmad=false: each float operation below rounds
+// once, in the order written, which is the order of the reference kernels
+// (reference src/collision.cu).  Together with IEEE division (nvcc's default
+// -prec-div=true) this makes the GPU results bit-identical to the reference's
+// float arithmetic, which is what the parity tests check.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lb {
+
+// ---------------------------------------------------------------- D3Q19 table
+// velocity set and order of the reference, src/collision.cu:463-478 and the
+// streaming pairs of src/streaming.cu:116-161
+__host__ __device__ constexpr int d3_cx(int k) {
+    return (k == 1 || (k >= 7 && k <= 10)) ? 1 : ((k == 2 || (k >= 11 && k <= 14)) ? -1 : 0);
+}
+__host__ __device__ constexpr int d3_cy(int k) {
+    return (k == 3 || k == 7 || k == 11 || k == 15 || k == 16) ? 1
+         : ((k == 4 || k == 8 || k == 12 || k == 17 || k == 18) ? -1 : 0);
+}
+__host__ __device__ constexpr int d3_cz(int k) {
+    return (k == 5 || k == 9 || k == 13 || k == 15 || k == 17) ? 1
+         : ((k == 6 || k == 10 || k == 14 || k == 16 || k == 18) ? -1 : 0);
+}
+__host__ __device__ constexpr int d3_opp(int k) {
+    return k == 0 ? 0 : (k <= 6 ? ((k & 1) ? k + 1 : k - 1)
+         : (k == 7 ? 12 : k == 8 ? 11 : k == 9 ? 14 : k == 10 ? 13 : k == 11 ? 8 : k == 12 ? 7
+         : k == 13 ? 10 : k == 14 ? 9 : k == 15 ? 18 : k == 16 ? 17 : k == 17 ? 16 : 15));
+}
+// slot of a streaming pair owned by the node itself (src/streaming.cu:127-161)
+__host__ __device__ constexpr bool d3_pos(int k) {
+    return k == 1 || k == 3 || k == 5 || k == 7 || k == 8 || k == 9 || k == 10 || k == 15 ||
+           k == 16;
+}
+
+// ---------------------------------------------------------------- D2Q9 table
+// x offset and ROW offset (physical +y is row-1), src/streaming.cu:44-68
+__host__ __device__ constexpr int d2_cx(int k) {
+    return (k == 1 || k == 5 || k == 8) ? 1 : ((k == 3 || k == 6 || k == 7) ? -1 : 0);
+}
+__host__ __device__ constexpr int d2_cr(int k) {
+    return (k == 2 || k == 5 || k == 6) ? -1 : ((k == 4 || k == 7 || k == 8) ? 1 : 0);
+}
+__host__ __device__ constexpr int d2_opp(int k) {
+    return k == 0 ? 0 : (k <= 4 ? ((k + 1) % 4 + 1) : ((k - 5 + 2) % 4 + 5));
+}
+__host__ __device__ constexpr bool d2_pos(int k) { return k == 1 || k == 2 || k == 5 || k == 6; }
+
+static_assert(d2_opp(1) == 3 && d2_opp(2) == 4 && d2_opp(3) == 1 && d2_opp(4) == 2, "d2 opp");
+static_assert(d2_opp(5) == 7 && d2_opp(6) == 8 && d2_opp(7) == 5 && d2_opp(8) == 6, "d2 opp");
+static_assert(d3_opp(7) == 12 && d3_opp(16) == 17 && d3_opp(5) == 6 && d3_opp(6) == 5, "d3 opp");
+
+// ---------------------------------------------------------------- bundles
+template <int Q> struct Pop {
+    float *f[Q];
+};
+template <int Q> struct CPop {
+    const float *__restrict__ f[Q];
+};
+
+// cell flag bits used by the kernels (the low two are the public LB_CELL_*)
+enum : uint8_t {
+    CELL_WALL = 0x01,
+    CELL_MOVING = 0x02,
+    CELL_NEAR_WALL = 0x04,   // fluid cell with at least one wall neighbour
+    CELL_SOLID_BOUND = 0x08, // reference mode: wall cell surrounded by walls
+};
+
+__device__ __forceinline__ int wrap_dec(int v, int n) { return v == 0 ? n - 1 : v - 1; }
+__device__ __forceinline__ int wrap_inc(int v, int n) { return v == n - 1 ? 0 : v + 1; }
+__device__ __forceinline__ int wrap_add(int v, int c, int n) {
+    return c > 0 ? wrap_inc(v, n) : (c < 0 ? wrap_dec(v, n) : v);
+}
+
+// streaming loads: read-only for the kernel's lifetime, touched once per step
+__device__ __forceinline__ float ld_stream(const float *p) { return __ldg(p); }
+
+// ---------------------------------------------------------------- BGK, D3Q19
+// relaxation towards the equilibrium at velocity (ux,uy,uz), reference
+// src/collision.cu:480-541 (same association of every term)
+__device__ __forceinline__ void d3q19_bgk(float (&g)[19], float ux, float uy, float uz,
+                                          float rho, float w0, float w1, float w7,
+                                          float tau_inv) {
+    const float uxsq = ux * ux, uysq = uy * uy, uzsq = uz * uz;
+    const float usq = uxsq + uysq + uzsq;
+    const float a0 = w0 * rho, a1 = w1 * rho, a7 = w7 * rho;
+    const float p7 = +ux + uy, p8 = +ux - uy, p9 = +ux + uz;
+    const float p10 = +ux - uz, p15 = +uy + uz, p16 = +uy - uz;
+    g[0]  = g[0]  - tau_inv * (g[0]  - a0 * (1.f - 1.5f * usq));
+    g[1]  = g[1]  - tau_inv * (g[1]  - a1 * (1.f + 3.f * ux + 4.5f * uxsq - 1.5f * usq));
+    g[2]  = g[2]  - tau_inv * (g[2]  - a1 * (1.f - 3.f * ux + 4.5f * uxsq - 1.5f * usq));
+    g[3]  = g[3]  - tau_inv * (g[3]  - a1 * (1.f + 3.f * uy + 4.5f * uysq - 1.5f * usq));
+    g[4]  = g[4]  - tau_inv * (g[4]  - a1 * (1.f - 3.f * uy + 4.5f * uysq - 1.5f * usq));
+    g[5]  = g[5]  - tau_inv * (g[5]  - a1 * (1.f + 3.f * uz + 4.5f * uzsq - 1.5f * usq));
+    g[6]  = g[6]  - tau_inv * (g[6]  - a1 * (1.f - 3.f * uz + 4.5f * uzsq - 1.5f * usq));
+    g[7]  = g[7]  - tau_inv * (g[7]  - a7 * (1.f + 3.f * p7  + 4.5f * p7  * p7  - 1.5f * usq));
+    g[8]  = g[8]  - tau_inv * (g[8]  - a7 * (1.f + 3.f * p8  + 4.5f * p8  * p8  - 1.5f * usq));
+    g[9]  = g[9]  - tau_inv * (g[9]  - a7 * (1.f + 3.f * p9  + 4.5f * p9  * p9  - 1.5f * usq));
+    g[10] = g[10] - tau_inv * (g[10] - a7 * (1.f + 3.f * p10 + 4.5f * p10 * p10 - 1.5f * usq));
+    g[11] = g[11] - tau_inv * (g[11] - a7 * (1.f - 3.f * p8  + 4.5f * p8  * p8  - 1.5f * usq));
+    g[12] = g[12] - tau_inv * (g[12] - a7 * (1.f - 3.f * p7  + 4.5f * p7  * p7  - 1.5f * usq));
+    g[13] = g[13] - tau_inv * (g[13] - a7 * (1.f - 3.f * p10 + 4.5f * p10 * p10 - 1.5f * usq));
+    g[14] = g[14] - tau_inv * (g[14] - a7 * (1.f - 3.f * p9  + 4.5f * p9  * p9  - 1.5f * usq));
+    g[15] = g[15] - tau_inv * (g[15] - a7 * (1.f + 3.f * p15 + 4.5f * p15 * p15 - 1.5f * usq));
+    g[16] = g[16] - tau_inv * (g[16] - a7 * (1.f + 3.f * p16 + 4.5f * p16 * p16 - 1.5f * usq));
+    g[17] = g[17] - tau_inv * (g[17] - a7 * (1.f - 3.f * p16 + 4.5f * p16 * p16 - 1.5f * usq));
+    g[18] = g[18] - tau_inv * (g[18] - a7 * (1.f - 3.f * p15 + 4.5f * p15 * p15 - 1.5f * usq));
+}
+
+// density and bare velocity, reference src/collision.cu:453-478
+__device__ __forceinline__ void d3q19_moments(const float (&g)[19], float &rho, float &ux,
+                                              float &uy, float &uz) {
+    rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8] + g[9] + g[10] + g[11] +
+          g[12] + g[13] + g[14] + g[15] + g[16] + g[17] + g[18];
+    ux = (g[1] + g[7] + g[8] + g[9] + g[10] - g[2] - g[11] - g[12] - g[13] - g[14]) / rho;
+    uy = (g[3] + g[7] + g[11] + g[15] + g[16] - g[4] - g[8] - g[12] - g[17] - g[18]) / rho;
+    uz = (g[5] + g[9] + g[13] + g[15] + g[17] - g[6] - g[10] - g[14] - g[16] - g[18]) / rho;
+}
+
+// Zou-He velocity inlet at the west face, reference src/collision.cu:412-430
+// (the reference's double literals promote these lines to FP64)
+__device__ __forceinline__ void d3q19_zou_he_west(float (&g)[19], float ux_in) {
+    const float a = g[0] + g[3] + g[4] + g[5] + g[6] + g[15] + g[16] + g[17] + g[18];
+    const float b = g[2] + g[11] + g[12] + g[13] + g[14];
+    const float rho = (float)(((double)a + 2. * (double)b) / (1. - (double)ux_in));
+    const float ru = rho * ux_in;
+    const float ty = g[3] + g[15] + g[16] - g[4] - g[17] - g[18];
+    const float tz = g[5] + g[11] + g[15] - g[6] - g[16] - g[18];
+    g[1]  = (float)((double)g[2]  + (1. / 3.) * (double)ru);
+    g[8]  = (float)((double)g[11] + (1. / 6.) * (double)ru + 0.5 * (double)ty);
+    g[7]  = (float)((double)g[12] + (1. / 6.) * (double)ru - 0.5 * (double)ty);
+    g[9]  = (float)((double)g[14] + (1. / 6.) * (double)ru - 0.5 * (double)tz);
+    g[10] = (float)((double)g[13] + (1. / 6.) * (double)ru + 0.5 * (double)tz);
+}
+
+// Zou-He pressure outlet at the east face, reference src/collision.cu:432-451;
+// the last two lines read the f11 written just before, as the reference does
+__device__ __forceinline__ void d3q19_zou_he_east(float (&g)[19], float rho_out) {
+    const float a = g[0] + g[3] + g[4] + g[5] + g[6] + g[15] + g[16] + g[17] + g[18];
+    const float b = g[1] + g[7] + g[8] + g[9] + g[10];
+    const float ux = (float)(-1. + ((double)a + 2. * (double)b) / (double)rho_out);
+    const float ru = rho_out * ux;
+    const float ty = g[3] + g[15] + g[16] - g[4] - g[17] - g[18];
+    g[2]  = (float)((double)g[1] - (1. / 3.) * (double)ru);
+    g[11] = (float)((double)g[8] - (1. / 6.) * (double)ru - 0.5 * (double)ty);
+    g[12] = (float)((double)g[7] - (1. / 6.) * (double)ru + 0.5 * (double)ty);
+    const float tz = g[5] + g[11] + g[15] - g[6] - g[16] - g[18];
+    g[14] = (float)((double)g[9]  - (1. / 6.) * (double)ru + 0.5 * (double)tz);
+    g[13] = (float)((double)g[10] - (1. / 6.) * (double)ru - 0.5 * (double)tz);
+}
+
+// ---------------------------------------------------------------- BGK, D2Q9
+// reference src/collision.cu:298-330
+__device__ __forceinline__ void d2q9_bgk(float (&g)[9], float ex, float ey, float rho, float w0,
+                                         float w1, float w5, float tau_inv) {
+    const float exsq = ex * ex, eysq = ey * ey;
+    const float esq = exsq + eysq;
+    const float a0 = w0 * rho, a1 = w1 * rho, a5 = w5 * rho;
+    const float u5 = +ex + ey, u6 = -ex + ey;
+    g[0] = g[0] - tau_inv * (g[0] - a0 * (1.f - 1.5f * esq));
+    g[1] = g[1] - tau_inv * (g[1] - a1 * (1.f + 3.f * ex + 4.5f * exsq - 1.5f * esq));
+    g[2] = g[2] - tau_inv * (g[2] - a1 * (1.f + 3.f * ey + 4.5f * eysq - 1.5f * esq));
+    g[3] = g[3] - tau_inv * (g[3] - a1 * (1.f - 3.f * ex + 4.5f * exsq - 1.5f * esq));
+    g[4] = g[4] - tau_inv * (g[4] - a1 * (1.f - 3.f * ey + 4.5f * eysq - 1.5f * esq));
+    g[5] = g[5] - tau_inv * (g[5] - a5 * (1.f + 3.f * u5 + 4.5f * u5 * u5 - 1.5f * esq));
+    g[6] = g[6] - tau_inv * (g[6] - a5 * (1.f + 3.f * u6 + 4.5f * u6 * u6 - 1.5f * esq));
+    g[7] = g[7] - tau_inv * (g[7] - a5 * (1.f - 3.f * u5 + 4.5f * u5 * u5 - 1.5f * esq));
+    g[8] = g[8] - tau_inv * (g[8] - a5 * (1.f - 3.f * u6 + 4.5f * u6 * u6 - 1.5f * esq));
+}
+
+__device__ __forceinline__ void d2q9_moments(const float (&g)[9], float &rho, float &ux,
+                                             float &uy) {
+    rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8];
+    ux = (g[1] - g[3] + g[5] - g[6] - g[7] + g[8]) / rho;
+    uy = (g[2] - g[4] + g[5] + g[6] - g[7] - g[8]) / rho;
+}
+
+// Zou-He west inlet / east outlet, reference src/collision.cu:210-262
+__device__ __forceinline__ void d2q9_zou_he_west(float (&g)[9], float ux_in) {
+    const float a = g[0] + g[2] + g[4], b = g[3] + g[7] + g[6];
+    const float r = (float)(((double)a + 2. * (double)b) / (1. - (double)ux_in));
+    const float ru = r * ux_in;
+    g[1] = (float)((double)g[3] + (2. / 3.) * (double)ru);
+    g[5] = (float)((double)g[7] + (1. / 6.) * (double)ru - 0.5 * (double)(g[2] - g[4]));
+    g[8] = (float)((double)g[6] + (1. / 6.) * (double)ru - 0.5 * (double)(g[4] - g[2]));
+}
+__device__ __forceinline__ void d2q9_zou_he_east(float (&g)[9], float rho_out) {
+    const float a = g[0] + g[2] + g[4], b = g[1] + g[5] + g[8];
+    const float vx = (float)(-1. + ((double)a + 2. * (double)b) / (double)rho_out);
+    const float ru = rho_out * vx;
+    g[3] = (float)((double)g[1] - (2. / 3.) * (double)ru);
+    g[7] = (float)((double)g[5] - (1. / 6.) * (double)ru + 0.5 * (double)(g[2] - g[4]));
+    g[6] = (float)((double)g[8] - (1. / 6.) * (double)ru + 0.5 * (double)(g[4] - g[2]));
+}
+
+// psi(rho) forms of the Shan-Chen pseudo-potential
+__device__ __forceinline__ float psi_ref(float rho) {  // src/collision.cu:293
+    return (float)(4. * exp(-200. / (double)rho));
+}
+__device__ __forceinline__ float psi_exp1(float rho) { return 1.f - expf(-rho); }
+
+}  // namespace lb

@@ -1,0 +1,464 @@
+// lb_context.cu -- the context API (include/lbgb300.h, part 2): one lattice
+// per context, populations in two library-owned structure-of-arrays sets that
+// the fused kernel ping-pongs between, batches of steps replayed from
+// captured CUDA graphs, FP64 reductions; plus the drop-in reductions and the
+// small device helpers.
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/lbgb300.h"
+#include "lb_kernels.cuh"
+
+using namespace lb;
+
+struct lb_ctx {
+    lb_config cfg{};
+    int Q = 0;
+    long N = 0, stride = 0;
+    float *pop[2] = {nullptr, nullptr};  // two population sets, Q arrays of `stride` floats each
+    int cur = 0;                         // index of the set holding the current state
+    uint8_t *flags = nullptr;            // CELL_* bits (native) or the solid array (reference)
+    uint8_t *sb = nullptr;               // reference mode: solid_bound
+    float *mom = nullptr;                // rho, ux, uy, uz (each `stride` floats)
+    float *sc = nullptr;                 // psi, ueq_x, ueq_y (D2Q9 Shan-Chen)
+    double *red = nullptr;               // reduction partials + result
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float corr[19] = {0};
+    bool flags_set = false;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(lb_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
+    return fail(c, LB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define LB_TRY(c, where, call)                                  \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(c, where, e_);  \
+    } while (0)
+
+const double W3[3] = {1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0};
+const double W2[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
+
+double d3_weight(int k) { return k == 0 ? W3[0] : (k <= 6 ? W3[1] : W3[2]); }
+double d2_weight(int k) { return k == 0 ? W2[0] : (k <= 4 ? W2[1] : W2[2]); }
+
+// the moving-wall term 6 w_k (c_k . u_wall), evaluated in double and rounded
+// to float (physical velocity components; for D2Q9 physical c_y = -row offset)
+void wall_corr(const lb_config &cfg, float *corr) {
+    if (cfg.lattice == LB_D3Q19) {
+        for (int k = 0; k < 19; k++) {
+            double dot = 0.0;
+            dot = dot + d3_cx(k) * (double)cfg.wall_u[0];
+            dot = dot + d3_cy(k) * (double)cfg.wall_u[1];
+            dot = dot + d3_cz(k) * (double)cfg.wall_u[2];
+            corr[k] = (float)(6.0 * d3_weight(k) * dot);
+        }
+    } else {
+        for (int k = 0; k < 9; k++) {
+            double dot = 0.0;
+            dot = dot + d2_cx(k) * (double)cfg.wall_u[0];
+            dot = dot + (-d2_cr(k)) * (double)cfg.wall_u[1];
+            corr[k] = (float)(6.0 * d2_weight(k) * dot);
+        }
+    }
+}
+
+float *pop_k(lb_ctx *c, int set, int k) { return c->pop[set] + (long)k * c->stride; }
+float *mom_k(lb_ctx *c, int i) { return c->mom + (long)i * c->stride; }
+
+// one time step from set `from` into set 1-from
+cudaError_t step_once(lb_ctx *c, int from, bool moments) {
+    const lb_config &g = c->cfg;
+    const int to = 1 - from;
+    if (c->Q == 19) {
+        D3Args a{};
+        for (int k = 0; k < 19; k++) {
+            a.src.f[k] = pop_k(c, from, k);
+            a.dst.f[k] = pop_k(c, to, k);
+        }
+        a.flags = c->flags; a.sb = c->sb;
+        a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2); a.uz = mom_k(c, 3);
+        a.W = g.nx; a.H = g.ny; a.D = g.nz; a.dev = 0; a.ndev = 1;
+        a.w0 = (float)W3[0]; a.w1 = (float)W3[1]; a.w7 = (float)W3[2];
+        a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
+        a.Fx = g.force[0]; a.Fy = g.force[1]; a.Fz = g.force[2];
+        memcpy(a.corr, c->corr, sizeof(a.corr));
+        c->launches += 1;
+        return launch_d3q19_fused(a, g.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE,
+                                  moments, false, c->stream);
+    }
+    D2Args a{};
+    for (int k = 0; k < 9; k++) {
+        a.src.f[k] = pop_k(c, from, k);
+        a.dst.f[k] = pop_k(c, to, k);
+    }
+    a.flags = c->flags; a.sb = c->sb;
+    a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2);
+    a.psi = c->sc; a.ueq_x = c->sc + c->stride; a.ueq_y = c->sc + 2 * c->stride;
+    a.W = g.nx; a.H = g.ny; a.dev = 0; a.ndev = 1;
+    a.w0 = (float)W2[0]; a.w1 = (float)W2[1]; a.w5 = (float)W2[2];
+    a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
+    a.Fx = g.force[0]; a.Fy = g.force[1]; a.G = g.G; a.Gads = g.G_ads;
+    a.psi_form = g.psi_form;
+    memcpy(a.corr, c->corr, sizeof(float) * 9);
+    const bool two = g.mode == LB_MODE_REFERENCE ? g.G < 0.f : g.G != 0.f;
+    c->launches += two ? 2 : 1;
+    return launch_d2q9_fused(a, g.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE, moments,
+                             false, c->stream);
+}
+
+int graph_for(lb_ctx *c, int from, cudaGraphExec_t *out) {
+    if (c->graph[from]) { *out = c->graph[from]; return LB_OK; }
+    cudaGraph_t graph;
+    const int64_t before = c->launches;
+    LB_TRY(c, "cudaStreamBeginCapture",
+           cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int set = from;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < c->cfg.graph_steps && e == cudaSuccess; i++) {
+        e = step_once(c, set, false);
+        set = 1 - set;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+    c->launches = before;  // capture launches nothing
+    if (e != cudaSuccess) return cuda_fail(c, "graph capture", e);
+    if (e2 != cudaSuccess) return cuda_fail(c, "cudaStreamEndCapture", e2);
+    e = cudaGraphInstantiate(&c->graph[from], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, "cudaGraphInstantiate", e);
+    *out = c->graph[from];
+    return LB_OK;
+}
+
+int launches_per_step(const lb_ctx *c) {
+    if (c->Q == 19) return 1;
+    return (c->cfg.mode == LB_MODE_REFERENCE ? c->cfg.G < 0.f : c->cfg.G != 0.f) ? 2 : 1;
+}
+
+// host-side flag preparation: native -> NEAR_WALL bits; reference -> 0/1
+// solid plus the reference's solid_bound rule (src/simulation_d3q19.cu:167-204,
+// src/simulation_d2q9.cu:318-334: x in 1..W-2 only, periodic in y and z)
+void prepare_flags(const lb_ctx *c, const uint8_t *in, std::vector<uint8_t> &flags,
+                   std::vector<uint8_t> &sb) {
+    const int W = c->cfg.nx, H = c->cfg.ny, D = c->cfg.nz, Q = c->Q;
+    const long N = c->N;
+    flags.assign(N, 0);
+    sb.assign(N, 0);
+    auto wrap = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
+    auto nb = [&](int x, int y, int z, int k, bool wrapx) -> long {
+        int xx, yy, zz;
+        if (Q == 19) { xx = x + d3_cx(k); yy = y + d3_cy(k); zz = z + d3_cz(k); }
+        else { xx = x + d2_cx(k); yy = y + d2_cr(k); zz = z; }
+        if (wrapx) xx = wrap(xx, W);
+        return xx + (long)W * (wrap(yy, H) + (long)H * wrap(zz, D));
+    };
+    if (c->cfg.mode == LB_MODE_REFERENCE) {
+        for (long o = 0; o < N; o++) flags[o] = in[o] ? 1 : 0;
+        for (int z = 0; z < D; z++)
+            for (int y = 0; y < H; y++)
+                for (int x = 1; x < W - 1; x++) {
+                    bool all = true;
+                    for (int k = 0; k < Q && all; k++) all = flags[nb(x, y, z, k, false)] != 0;
+                    sb[x + (long)W * (y + (long)H * z)] = all ? 1 : 0;
+                }
+        return;
+    }
+    for (long o = 0; o < N; o++)
+        flags[o] = (in[o] & CELL_WALL) ? (in[o] & (CELL_WALL | CELL_MOVING)) : 0;
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                const long o = x + (long)W * (y + (long)H * z);
+                if (flags[o] & CELL_WALL) continue;
+                for (int k = 1; k < Q; k++)
+                    if (flags[nb(x, y, z, k, true)] & CELL_WALL) {
+                        flags[o] |= CELL_NEAR_WALL;
+                        break;
+                    }
+            }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *lb_version(void) { return "lbgb300 0.1 (sm_103a)"; }
+
+int lb_config_default(lb_config *cfg, int lattice, int nx, int ny, int nz) {
+    if (!cfg) return LB_ERR_ARG;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->lattice = lattice;
+    cfg->nx = nx; cfg->ny = ny; cfg->nz = lattice == LB_D2Q9 ? 1 : nz;
+    cfg->mode = LB_MODE_NATIVE;
+    cfg->storage = LB_STORE_F32;
+    cfg->tau_inv = 1.f;
+    cfg->rho_out = 1.f;
+    cfg->psi_form = LB_PSI_EXP1;
+    cfg->graph_steps = 64;
+    return LB_OK;
+}
+
+int lb_create(const lb_config *cfg, lb_ctx **out) {
+    if (!cfg || !out) return LB_ERR_ARG;
+    *out = nullptr;
+    if (cfg->lattice != LB_D2Q9 && cfg->lattice != LB_D3Q19) return LB_ERR_ARG;
+    if (cfg->nx < 1 || cfg->ny < 1 || cfg->nz < 1 || (cfg->lattice == LB_D2Q9 && cfg->nz != 1))
+        return LB_ERR_ARG;
+    if (cfg->mode != LB_MODE_REFERENCE && cfg->mode != LB_MODE_NATIVE) return LB_ERR_ARG;
+    if (cfg->storage != LB_STORE_F32) return LB_ERR_ARG;  // deviation storage: lb_create16
+    const long N = (long)cfg->nx * cfg->ny * cfg->nz;
+    if (N > (1L << 31) - 64) return LB_ERR_ARG;  // 32-bit node offsets in the kernels
+    lb_ctx *c = new lb_ctx;
+    c->cfg = *cfg;
+    if (c->cfg.graph_steps <= 0) c->cfg.graph_steps = 64;
+    c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
+    c->Q = cfg->lattice;
+    c->N = N;
+    c->stride = (N + 63) / 64 * 64;  // each population array starts on a 256-byte boundary
+    wall_corr(c->cfg, c->corr);
+    cudaError_t e = cudaSuccess;
+    const size_t pbytes = sizeof(float) * c->stride * c->Q;
+    if (e == cudaSuccess) e = cudaMalloc(&c->pop[0], pbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->pop[1], pbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->flags, c->stride);
+    if (e == cudaSuccess) e = cudaMalloc(&c->sb, c->stride);
+    if (e == cudaSuccess) e = cudaMalloc(&c->mom, sizeof(float) * c->stride * 4);
+    if (e == cudaSuccess && c->Q == 9) e = cudaMalloc(&c->sc, sizeof(float) * c->stride * 3);
+    if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 8));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->flags, 0, c->stride, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->sb, 0, c->stride, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->mom, 0, sizeof(float) * c->stride * 4, c->stream);
+    if (e == cudaSuccess && c->sc) e = cudaMemsetAsync(c->sc, 0, sizeof(float) * c->stride * 3, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        lb_destroy(c);
+        return e == cudaErrorMemoryAllocation ? LB_ERR_NOMEM : LB_ERR_CUDA;
+    }
+    *out = c;
+    return LB_OK;
+}
+
+int lb_destroy(lb_ctx *c) {
+    if (!c) return LB_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < 2; i++) {
+        if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
+        if (c->pop[i]) cudaFree(c->pop[i]);
+    }
+    if (c->flags) cudaFree(c->flags);
+    if (c->sb) cudaFree(c->sb);
+    if (c->mom) cudaFree(c->mom);
+    if (c->sc) cudaFree(c->sc);
+    if (c->red) cudaFree(c->red);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return LB_OK;
+}
+
+const char *lb_error(const lb_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int lb_set_flags(lb_ctx *c, const uint8_t *flags) {
+    if (!c || !flags) return fail(c, LB_ERR_ARG, "lb_set_flags: null argument");
+    std::vector<uint8_t> f, sb;
+    prepare_flags(c, flags, f, sb);
+    LB_TRY(c, "lb_set_flags", cudaMemcpyAsync(c->flags, f.data(), c->N, cudaMemcpyHostToDevice, c->stream));
+    LB_TRY(c, "lb_set_flags", cudaMemcpyAsync(c->sb, sb.data(), c->N, cudaMemcpyHostToDevice, c->stream));
+    LB_TRY(c, "lb_set_flags", cudaStreamSynchronize(c->stream));
+    c->flags_set = true;
+    return LB_OK;
+}
+
+int lb_set_populations(lb_ctx *c, const float *f) {
+    if (!c || !f) return fail(c, LB_ERR_ARG, "lb_set_populations: null argument");
+    for (int k = 0; k < c->Q; k++)
+        LB_TRY(c, "lb_set_populations",
+               cudaMemcpyAsync(pop_k(c, c->cur, k), f + (long)k * c->N, sizeof(float) * c->N,
+                               cudaMemcpyHostToDevice, c->stream));
+    LB_TRY(c, "lb_set_populations", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_get_populations(lb_ctx *c, float *f) {
+    if (!c || !f) return fail(c, LB_ERR_ARG, "lb_get_populations: null argument");
+    for (int k = 0; k < c->Q; k++)
+        LB_TRY(c, "lb_get_populations",
+               cudaMemcpyAsync(f + (long)k * c->N, pop_k(c, c->cur, k), sizeof(float) * c->N,
+                               cudaMemcpyDeviceToHost, c->stream));
+    LB_TRY(c, "lb_get_populations", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const float *uy,
+                        const float *uz) {
+    if (!c) return LB_ERR_ARG;
+    const float *src[4] = {rho, ux, uy, uz};
+    const float *dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int i = 0; i < 4; i++) {
+        if (!src[i] || (i == 3 && c->Q == 9)) continue;
+        LB_TRY(c, "lb_init_equilibrium",
+               cudaMemcpyAsync(mom_k(c, i), src[i], sizeof(float) * c->N, cudaMemcpyHostToDevice,
+                               c->stream));
+        dev[i] = mom_k(c, i);
+    }
+    cudaError_t e;
+    if (c->Q == 19) {
+        Pop<19> p;
+        for (int k = 0; k < 19; k++) p.f[k] = pop_k(c, c->cur, k);
+        e = launch_d3q19_equilibrium(p, dev[0], dev[1], dev[2], dev[3], (int)c->N, (float)W3[0],
+                                     (float)W3[1], (float)W3[2], c->stream);
+    } else {
+        Pop<9> p;
+        for (int k = 0; k < 9; k++) p.f[k] = pop_k(c, c->cur, k);
+        e = launch_d2q9_equilibrium(p, dev[0], dev[1], dev[2], (int)c->N, (float)W2[0],
+                                    (float)W2[1], (float)W2[2], c->stream);
+    }
+    LB_TRY(c, "lb_init_equilibrium", e);
+    c->launches += 1;
+    LB_TRY(c, "lb_init_equilibrium", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_step(lb_ctx *c, int nsteps) {
+    if (!c || nsteps < 0) return fail(c, LB_ERR_ARG, "lb_step: bad argument");
+    if (nsteps == 0) return LB_OK;
+    int rest = nsteps - 1;  // the last step also writes the moment fields
+    while (rest >= c->cfg.graph_steps) {
+        cudaGraphExec_t g;
+        int rc = graph_for(c, c->cur, &g);
+        if (rc != LB_OK) return rc;
+        LB_TRY(c, "cudaGraphLaunch", cudaGraphLaunch(g, c->stream));
+        c->launches += (int64_t)c->cfg.graph_steps * launches_per_step(c);
+        rest -= c->cfg.graph_steps;
+    }
+    for (; rest > 0; rest--) {
+        LB_TRY(c, "lb_step", step_once(c, c->cur, false));
+        c->cur = 1 - c->cur;
+    }
+    LB_TRY(c, "lb_step", step_once(c, c->cur, true));
+    c->cur = 1 - c->cur;
+    return LB_OK;
+}
+
+int lb_get_moments(lb_ctx *c, float *rho, float *ux, float *uy, float *uz) {
+    if (!c) return LB_ERR_ARG;
+    float *dst[4] = {rho, ux, uy, uz};
+    for (int i = 0; i < 4; i++) {
+        if (!dst[i] || (i == 3 && c->Q == 9)) continue;
+        LB_TRY(c, "lb_get_moments",
+               cudaMemcpyAsync(dst[i], mom_k(c, i), sizeof(float) * c->N, cudaMemcpyDeviceToHost,
+                               c->stream));
+    }
+    LB_TRY(c, "lb_get_moments", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_reduce(lb_ctx *c, double out[7]) {
+    if (!c || !out) return LB_ERR_ARG;
+    double *res = c->red + reduce_partials_size();
+    LB_TRY(c, "lb_reduce",
+           launch_reduce(mom_k(c, 0), mom_k(c, 1), mom_k(c, 2), c->Q == 19 ? mom_k(c, 3) : nullptr,
+                         c->flags, CELL_WALL, c->N, c->red, res, c->stream));
+    c->launches += 2;
+    LB_TRY(c, "lb_reduce", cudaMemcpyAsync(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
+    LB_TRY(c, "lb_reduce", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_synchronize(lb_ctx *c) {
+    if (!c) return LB_ERR_ARG;
+    LB_TRY(c, "lb_synchronize", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_time_steps(lb_ctx *c, int nsteps, float *ms) {
+    if (!c || !ms) return LB_ERR_ARG;
+    LB_TRY(c, "lb_time_steps", cudaEventRecord(c->ev0, c->stream));
+    int rc = lb_step(c, nsteps);
+    if (rc != LB_OK) return rc;
+    LB_TRY(c, "lb_time_steps", cudaEventRecord(c->ev1, c->stream));
+    LB_TRY(c, "lb_time_steps", cudaEventSynchronize(c->ev1));
+    LB_TRY(c, "lb_time_steps", cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return LB_OK;
+}
+
+int64_t lb_launch_count(const lb_ctx *c) { return c ? c->launches : -1; }
+
+int lb_wall_correction(const lb_ctx *c, float *corr) {
+    if (!c || !corr) return LB_ERR_ARG;
+    memcpy(corr, c->corr, sizeof(float) * c->Q);
+    return LB_OK;
+}
+
+// ----------------------------------------------------------------- drop-in reductions
+static std::mutex g_red_mu;
+static double *g_red = nullptr;  // partials + result, allocated on first use
+
+static int abi_reduce(const float *rho, const float *ux, const float *uy, const float *uz,
+                      const void *solid, long N, double out[7]) {
+    std::lock_guard<std::mutex> l(g_red_mu);
+    if (!g_red && cudaMalloc(&g_red, sizeof(double) * (reduce_partials_size() + 8)) != cudaSuccess)
+        return LB_ERR_NOMEM;
+    double *res = g_red + reduce_partials_size();
+    cudaError_t e = launch_reduce(rho, ux, uy, uz, reinterpret_cast<const uint8_t *>(solid), 0xff,
+                                  N, g_red, res, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+
+int lb_reduce_d3q19(const DataD3Q19 *d, double out[7]) {
+    if (!d || !out) return LB_ERR_ARG;
+    return abi_reduce(d->rho, d->ux, d->uy, d->uz, d->solid,
+                      (long)d->width * d->height * d->depth, out);
+}
+
+int lb_reduce_d2q9(const DataD2Q9 *d, double out[7]) {
+    if (!d || !out) return LB_ERR_ARG;
+    return abi_reduce(d->rho, d->ux, d->uy, nullptr, d->solid, (long)d->width * d->height, out);
+}
+
+// ----------------------------------------------------------------- device helpers
+int lb_device_count(int *n) {
+    if (!n) return LB_ERR_ARG;
+    return cudaGetDeviceCount(n) == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+int lb_malloc(void **p, size_t bytes) {
+    if (!p) return LB_ERR_ARG;
+    return cudaMalloc(p, bytes) == cudaSuccess ? LB_OK : LB_ERR_NOMEM;
+}
+int lb_free(void *p) { return cudaFree(p) == cudaSuccess ? LB_OK : LB_ERR_CUDA; }
+int lb_malloc_host(void **p, size_t bytes) {
+    if (!p) return LB_ERR_ARG;
+    return cudaMallocHost(p, bytes) == cudaSuccess ? LB_OK : LB_ERR_NOMEM;
+}
+int lb_free_host(void *p) { return cudaFreeHost(p) == cudaSuccess ? LB_OK : LB_ERR_CUDA; }
+int lb_memcpy_h2d(void *dst, const void *src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+int lb_memcpy_d2h(void *dst, const void *src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+int lb_memset(void *dst, int value, size_t bytes) {
+    return cudaMemset(dst, value, bytes) == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+int lb_device_synchronize(void) {
+    return cudaDeviceSynchronize() == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,269 @@
+// lb_d3q19.cu -- D3Q19 kernels: the fused pull-stream + collide step (the hot
+// path), and the reference-exact standalone streaming / collision / border
+// kernels behind the drop-in entry points.
+//
+// Layout: structure of arrays, one float array per population, node index
+// o = x + W*(y + H*z) (reference src/streaming.cu:98).  A thread owns one
+// node; a block covers a run of x at fixed (y, z), so every population load
+// and store of a warp is one coalesced 128-byte row (shifted by one element
+// for populations with c_x != 0).
+#include "lb_kernels.cuh"
+
+namespace lb {
+
+// offset from node o to its neighbour o + c for c in {-1, 0, +1}^3, periodic
+struct Nbr3 {
+    int xm, xp, ym, yp, zm, zp;  // offsets of the -/+ neighbour per axis
+    __device__ __forceinline__ Nbr3(int x, int y, int z, int W, int H, int D) {
+        const int WH = W * H;
+        xm = x == 0 ? W - 1 : -1;
+        xp = x == W - 1 ? -(W - 1) : 1;
+        ym = y == 0 ? (H - 1) * W : -W;
+        yp = y == H - 1 ? -(H - 1) * W : W;
+        zm = z == 0 ? (D - 1) * WH : -WH;
+        zp = z == D - 1 ? -(D - 1) * WH : WH;
+    }
+    // offset of o + (cx, cy, cz)
+    __device__ __forceinline__ int off(int cx, int cy, int cz) const {
+        return (cx > 0 ? xp : (cx < 0 ? xm : 0)) + (cy > 0 ? yp : (cy < 0 ? ym : 0)) +
+               (cz > 0 ? zp : (cz < 0 ? zm : 0));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Fused step.  Pull: population k of node o comes from o - c_k.
+//  * fluid node: pull all 18, (reference mode) Zou-He on the x faces,
+//    moments, (native) force shift, BGK, store to dst at o.
+//  * reference mode, solid node: reproduces the reference's full-way
+//    bounce-back storage.  Slot m of a solid node receives, by the swap
+//    streaming of src/streaming.cu, the population opp(m) leaving
+//    o + c_m, i.e. src[opp(m)][o + c_m] -- unless the node that owns that
+//    swap pair is solid_bound (o itself for the positive slots, o + c_m for
+//    the others), in which case the slot keeps its value.
+//  * native mode: a fluid node whose upstream neighbour is a wall takes its
+//    own outgoing opposite population (half-way bounce-back), minus the
+//    moving-wall term corr[opp(k)].  Wall nodes are not updated.
+// ---------------------------------------------------------------------------
+template <int MODE, bool MOM, bool PLOT>
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= a.W) return;
+    const int o = x + a.W * (y + a.H * z);
+    const uint8_t fl = a.flags[o];
+    const Nbr3 n(x, y, z, a.W, a.H, a.D);
+
+    if (MODE == MODE_REF && (fl & CELL_WALL)) {
+        const bool sb_self = a.sb[o] != 0;
+#pragma unroll
+        for (int m = 0; m < 19; m++) {
+            float v;
+            if (m == 0) {
+                v = ld_stream(a.src.f[0] + o);
+            } else {
+                const int on = o + n.off(d3_cx(m), d3_cy(m), d3_cz(m));
+                const bool resp_sb = d3_pos(m) ? sb_self : (a.sb[on] != 0);
+                v = resp_sb ? ld_stream(a.src.f[m] + o) : ld_stream(a.src.f[d3_opp(m)] + on);
+            }
+            a.dst.f[m][o] = v;
+        }
+        if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+        if (PLOT) a.plot[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    if (MODE == MODE_NATIVE && (fl & CELL_WALL)) {
+        if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+        return;
+    }
+
+    float g[19];
+    if (MODE == MODE_NATIVE && (fl & CELL_NEAR_WALL)) {
+#pragma unroll
+        for (int k = 0; k < 19; k++) {
+            const int up = o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k));
+            const uint8_t fu = k == 0 ? 0 : a.flags[up];
+            if (fu & CELL_WALL) {
+                const float v = ld_stream(a.src.f[d3_opp(k)] + o);
+                g[k] = (fu & CELL_MOVING) ? v - a.corr[d3_opp(k)] : v;
+            } else {
+                g[k] = ld_stream(a.src.f[k] + up);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 19; k++)
+            g[k] = ld_stream(a.src.f[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)));
+    }
+
+    if (MODE == MODE_REF) {
+        if (x == 0 && a.dev == 0)
+            d3q19_zou_he_west(g, a.ux_in);
+        else if (x == a.W - 1 && a.dev == a.ndev - 1)
+            d3q19_zou_he_east(g, a.rho_out);
+    }
+    float rho, ux, uy, uz;
+    d3q19_moments(g, rho, ux, uy, uz);
+    if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+    if (PLOT) a.plot[o] = make_float4(ux, uy, uz, rho);
+    float ex = ux, ey = uy, ez = uz;
+    if (MODE == MODE_NATIVE) {
+        // velocity-shift forcing, the form of reference src/collision.cu:280-284
+        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
+        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
+        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * a.tau_inv);
+    }
+    d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+#pragma unroll
+    for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+}
+
+// ---------------------------------------------------------------------------
+// Reference-exact standalone streaming, src/streaming.cu:84-163: in-place
+// swap of f_k(o) and f_opp(k)(o + c_k) for the nine owned slots.  Every
+// (node, slot) belongs to exactly one pair and each pair to exactly one
+// thread, so the in-place update has no race.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_stream_swap_kernel(Pop<19> p,
+                                                                    const uint8_t *sb, int W,
+                                                                    int H, int D) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const int o = x + W * (y + H * z);
+    if (sb[o]) return;
+    const Nbr3 n(x, y, z, W, H, D);
+#pragma unroll
+    for (int k = 1; k < 19; k++) {
+        if (!d3_pos(k)) continue;
+        const int on = o + n.off(d3_cx(k), d3_cy(k), d3_cz(k));
+        const float t = p.f[k][o];
+        p.f[k][o] = p.f[d3_opp(k)][on];
+        p.f[d3_opp(k)][on] = t;
+    }
+}
+
+// Reference-exact standalone collision, src/collision.cu:357-552.
+template <bool PLOT>
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_collide_kernel(const D3Args a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= a.W) return;
+    const int o = x + a.W * (y + a.H * z);
+    if (a.flags[o]) {
+        a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f;
+        if (PLOT) a.plot[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    float g[19];
+    // local swap back to natural slot order ("bounce-back" in the reference)
+#pragma unroll
+    for (int k = 0; k < 19; k++) g[k] = a.dst.f[d3_opp(k)][o];
+    if (x == 0 && a.dev == 0)
+        d3q19_zou_he_west(g, a.ux_in);
+    else if (x == a.W - 1 && a.dev == a.ndev - 1)
+        d3q19_zou_he_east(g, a.rho_out);
+    float rho, ux, uy, uz;
+    d3q19_moments(g, rho, ux, uy, uz);
+    a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho;
+    if (PLOT) a.plot[o] = make_float4(ux, uy, uz, rho);
+    d3q19_bgk(g, ux, uy, uz, rho, a.w0, a.w1, a.w7, a.tau_inv);
+#pragma unroll
+    for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+}
+
+// x-face pack / unpack, src/get_border.cu:59-98 and src/apply_border.cu:58-97;
+// one thread per face node instead of a full-grid launch
+__global__ void d3q19_get_border_kernel(CPop<19> p, Pop<10> border, int W, int H, int D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // y + z*H
+    if (i >= H * D) return;
+    const int y = i % H, z = i / H;
+    const int oe = (W - 1) + W * (y + H * z), ow = W * (y + H * z);
+    border.f[0][i] = p.f[1][oe];  border.f[1][i] = p.f[7][oe];  border.f[2][i] = p.f[8][oe];
+    border.f[3][i] = p.f[9][oe];  border.f[4][i] = p.f[10][oe];
+    border.f[5][i] = p.f[2][ow];  border.f[6][i] = p.f[11][ow]; border.f[7][i] = p.f[12][ow];
+    border.f[8][i] = p.f[13][ow]; border.f[9][i] = p.f[14][ow];
+}
+
+__global__ void d3q19_apply_border_kernel(Pop<19> p, CPop<10> nb, int W, int H, int D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= H * D) return;
+    const int y = i % H, z = i / H;
+    const int oe = (W - 1) + W * (y + H * z), ow = W * (y + H * z);
+    p.f[2][ow] = nb.f[5][i];  p.f[11][ow] = nb.f[6][i]; p.f[12][ow] = nb.f[7][i];
+    p.f[13][ow] = nb.f[8][i]; p.f[14][ow] = nb.f[9][i];
+    p.f[1][oe] = nb.f[0][i];  p.f[7][oe] = nb.f[1][i];  p.f[8][oe] = nb.f[2][i];
+    p.f[9][oe] = nb.f[3][i];  p.f[10][oe] = nb.f[4][i];
+}
+
+// equilibrium from moment fields (BGK with tau_inv = 1 from zero populations
+// yields the equilibrium in the BGK's own operation order)
+__global__ void d3q19_equilibrium_kernel(Pop<19> p, const float *rho, const float *ux,
+                                         const float *uy, const float *uz, int N, float w0,
+                                         float w1, float w7) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= N) return;
+    float g[19];
+#pragma unroll
+    for (int k = 0; k < 19; k++) g[k] = 0.f;
+    d3q19_bgk(g, ux ? ux[o] : 0.f, uy ? uy[o] : 0.f, uz ? uz[o] : 0.f, rho ? rho[o] : 1.f, w0,
+              w1, w7, 1.f);
+#pragma unroll
+    for (int k = 0; k < 19; k++) p.f[k][o] = g[k];
+}
+
+// ---------------------------------------------------------------- launchers
+static dim3 grid_of(int W, int H, int D) { return dim3((W + D3_BLOCK - 1) / D3_BLOCK, H, D); }
+
+cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, cudaStream_t s) {
+    const dim3 g = grid_of(a.W, a.H, a.D), b(D3_BLOCK);
+#define LB_D3_CASE(M, MO, PL)                                                    \
+    if (mode == M && mom == MO && plot == PL) {                                  \
+        d3q19_fused_kernel<M, MO, PL><<<g, b, 0, s>>>(a);                       \
+        return cudaGetLastError();                                               \
+    }
+    LB_D3_CASE(MODE_REF, true, true)
+    LB_D3_CASE(MODE_REF, true, false)
+    LB_D3_CASE(MODE_REF, false, false)
+    LB_D3_CASE(MODE_NATIVE, true, false)
+    LB_D3_CASE(MODE_NATIVE, false, false)
+    LB_D3_CASE(MODE_NATIVE, true, true)
+#undef LB_D3_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_d3q19_stream_swap(const Pop<19> &p, const uint8_t *sb, int W, int H, int D,
+                                     cudaStream_t s) {
+    d3q19_stream_swap_kernel<<<grid_of(W, H, D), D3_BLOCK, 0, s>>>(p, sb, W, H, D);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_collide(const D3Args &a, bool plot, cudaStream_t s) {
+    if (plot)
+        d3q19_collide_kernel<true><<<grid_of(a.W, a.H, a.D), D3_BLOCK, 0, s>>>(a);
+    else
+        d3q19_collide_kernel<false><<<grid_of(a.W, a.H, a.D), D3_BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_get_border(const CPop<19> &p, const Pop<10> &b, int W, int H, int D,
+                                    cudaStream_t s) {
+    const int n = H * D;
+    d3q19_get_border_kernel<<<(n + 255) / 256, 256, 0, s>>>(p, b, W, H, D);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_apply_border(const Pop<19> &p, const CPop<10> &nb, int W, int H, int D,
+                                      cudaStream_t s) {
+    const int n = H * D;
+    d3q19_apply_border_kernel<<<(n + 255) / 256, 256, 0, s>>>(p, nb, W, H, D);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_equilibrium(const Pop<19> &p, const float *rho, const float *ux,
+                                     const float *uy, const float *uz, int N, float w0, float w1,
+                                     float w7, cudaStream_t s) {
+    d3q19_equilibrium_kernel<<<(N + 255) / 256, 256, 0, s>>>(p, rho, ux, uy, uz, N, w0, w1, w7);
+    return cudaGetLastError();
+}
+
+}  // namespace lb

@@ -1,0 +1,79 @@
+// lb_kernels.cuh -- kernel argument bundles and launcher prototypes shared by
+// the kernel files (lb_d3q19.cu, lb_d2q9.cu, lb_reduce.cu) and the host layers
+// (lb_abi.cu, lb_context.cu).
+#pragma once
+
+#include "lb_common.cuh"
+
+namespace lb {
+
+enum { MODE_REF = 0, MODE_NATIVE = 1 };
+
+constexpr int D3_BLOCK = 128;  // threads per block along x (D3Q19)
+constexpr int D2_BLOCK = 128;  // threads per block along x (D2Q9)
+
+struct D3Args {
+    CPop<19> src;           // populations at the start of the step
+    Pop<19> dst;            // populations after the step (== src for in-place kernels)
+    const uint8_t *flags;   // native: CELL_* bits; reference: the solid array (0/1)
+    const uint8_t *sb;      // reference: solid_bound (0/1)
+    float *ux, *uy, *uz, *rho;
+    float4 *plot;
+    int W, H, D, dev, ndev;
+    float w0, w1, w7, tau_inv, ux_in, rho_out, Fx, Fy, Fz;
+    float corr[19];         // moving-wall momentum term per direction
+};
+
+struct D2Args {
+    CPop<9> src;
+    Pop<9> dst;
+    const uint8_t *flags;
+    const uint8_t *sb;
+    float *ux, *uy, *rho;
+    float4 *plot;
+    float *psi, *ueq_x, *ueq_y;
+    int W, H, dev, ndev;
+    float w0, w1, w5, tau_inv, ux_in, rho_out, Fx, Fy, G, Gads;
+    int psi_form;
+    float corr[9];
+};
+
+// D3Q19
+cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, cudaStream_t s);
+cudaError_t launch_d3q19_stream_swap(const Pop<19> &p, const uint8_t *sb, int W, int H, int D,
+                                     cudaStream_t s);
+cudaError_t launch_d3q19_collide(const D3Args &a, bool plot, cudaStream_t s);
+cudaError_t launch_d3q19_get_border(const CPop<19> &p, const Pop<10> &b, int W, int H, int D,
+                                    cudaStream_t s);
+cudaError_t launch_d3q19_apply_border(const Pop<19> &p, const CPop<10> &nb, int W, int H, int D,
+                                      cudaStream_t s);
+cudaError_t launch_d3q19_equilibrium(const Pop<19> &p, const float *rho, const float *ux,
+                                     const float *uy, const float *uz, int N, float w0, float w1,
+                                     float w7, cudaStream_t s);
+
+// D2Q9
+cudaError_t launch_d2q9_fused(const D2Args &a, int mode, bool mom, bool plot, cudaStream_t s);
+cudaError_t launch_d2q9_stream_swap(const Pop<9> &p, const uint8_t *sb, int W, int H,
+                                    cudaStream_t s);
+cudaError_t launch_d2q9_collide(const D2Args &a, bool plot, cudaStream_t s);
+cudaError_t launch_d2q9_get_border(const CPop<9> &p, const Pop<6> &b, int W, int H,
+                                   cudaStream_t s);
+cudaError_t launch_d2q9_apply_border(const Pop<9> &p, const CPop<6> &nb, int W, int H,
+                                     cudaStream_t s);
+cudaError_t launch_d2q9_equilibrium(const Pop<9> &p, const float *rho, const float *ux,
+                                    const float *uy, int N, float w0, float w1, float w5,
+                                    cudaStream_t s);
+
+// probes and reductions
+cudaError_t launch_read_value(const float *plot, const float *ux, const float *uy,
+                             const float *uz, const float *rho, float *value, long o,
+                             cudaStream_t s);
+// out_dev[7] = {mass, mom_x, mom_y, mom_z, kinetic energy, max|u|, n_fluid};
+// nodes with (solid[o] & mask) != 0 are skipped; partials must hold
+// reduce_partials_size() doubles
+int reduce_partials_size();
+cudaError_t launch_reduce(const float *rho, const float *ux, const float *uy, const float *uz,
+                          const uint8_t *solid, uint8_t mask, long N, double *partials,
+                          double *out_dev, cudaStream_t s);
+
+}  // namespace lb
