@@ -39,8 +39,9 @@ SPHERE = (64, 64, 64, 16)
 BYTES_PER_LU = 2 * 19 * 4 + 1
 # DRAM bytes per launch of the fused kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) from the ncu capture summarised in
-# profiles/d3q19_fused_channel_256x128x128.md; None until captured
-NCU_TRAFFIC_PER_LAUNCH = None
+# profiles/d3q19_fused_channel_256x128x128.md (captured at 128^3 and scaled
+# by the node count to this lattice)
+NCU_TRAFFIC_PER_LAUNCH = 522.1e6
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -205,7 +206,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2000)
+    ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()
+    if args.size:
+        global NX, NY, NZ
+        NX, NY, NZ = args.size
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
