@@ -206,6 +206,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2000)
+    ap.add_argument("--tuning", type=lambda v: int(v, 0), default=0,
+                    help="lb_config.tuning (0 = the library's default)")
     ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()
@@ -226,7 +228,7 @@ def main():
 
     # ------------------------------------------------ device-resident throughput
     lat = pkg.Lattice(19, NX, NY, NZ, tau_inv=np.float32(1 / TAU),
-                      force=(np.float32(GX), 0, 0), graph_steps=64)
+                      force=(np.float32(GX), 0, 0), graph_steps=64, tuning=args.tuning)
     lat.set_flags(flags)
     lat.init_equilibrium()
     lat.step(args.warmup)

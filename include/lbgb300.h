@@ -147,6 +147,13 @@ typedef enum {
 #define LB_CELL_WALL 0x01u
 #define LB_CELL_MOVING 0x02u /* with LB_CELL_WALL: wall moving with config.wall_u */
 
+/* launch tuning (lb_config.tuning); results do not depend on it */
+#define LB_TUNE_DEFAULT 0      /* the library's measured choice */
+#define LB_TUNE_EXPLICIT 0x100 /* use exactly the bits below */
+#define LB_TUNE_REVERSE 0x001  /* sweep the lattice in the opposite order on every
+                                  other step, so a step starts where the previous
+                                  one ended and its last writes are still in L2 */
+
 typedef struct {
     int lattice;        /* LB_D2Q9 or LB_D3Q19 */
     int nx, ny, nz;     /* nodes; nz = 1 for D2Q9 */
@@ -160,6 +167,7 @@ typedef struct {
     float G, G_ads;     /* Shan-Chen interaction and adhesion strengths (0 = off) */
     int psi_form;       /* LB_PSI_* */
     int graph_steps;    /* steps per captured CUDA graph in lb_step (0 = default 64) */
+    int tuning;         /* LB_TUNE_* bits; LB_TUNE_DEFAULT picks the measured best */
 } lb_config;
 
 typedef struct lb_ctx lb_ctx;

@@ -64,7 +64,8 @@ class lb_config(ctypes.Structure):
                 ("tau_inv", ctypes.c_float), ("force", ctypes.c_float * 3),
                 ("u_in", ctypes.c_float * 3), ("rho_out", ctypes.c_float),
                 ("wall_u", ctypes.c_float * 3), ("G", ctypes.c_float), ("G_ads", ctypes.c_float),
-                ("psi_form", ctypes.c_int), ("graph_steps", ctypes.c_int)]
+                ("psi_form", ctypes.c_int), ("graph_steps", ctypes.c_int),
+                ("tuning", ctypes.c_int)]
 
 
 class lb_run_params_d3q19(ctypes.Structure):
@@ -80,6 +81,7 @@ LB_STORE_F32, LB_STORE_F16, LB_STORE_BF16 = 0, 1, 2
 LB_PSI_REF, LB_PSI_EXP1 = 0, 1
 LB_CELL_FLUID, LB_CELL_WALL, LB_CELL_MOVING = 0, 1, 2
 LB_ABI_STANDALONE, LB_ABI_FUSED = 0, 1
+LB_TUNE_DEFAULT, LB_TUNE_EXPLICIT, LB_TUNE_REVERSE = 0, 0x100, 0x001
 
 _c = ctypes
 # (name, restype, argtypes) of every exported C symbol declared in include/lbgb300.h

@@ -28,6 +28,7 @@ struct lb_ctx {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float corr[19] = {0};
+    int tune = 0;                        // LB_TUNE_* bits in effect
     bool flags_set = false;
     int64_t launches = 0;
     std::string err;
@@ -47,6 +48,9 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
         cudaError_t e_ = (call);                                \
         if (e_ != cudaSuccess) return cuda_fail(c, where, e_);  \
     } while (0)
+
+// launch tuning used when the caller leaves lb_config.tuning at LB_TUNE_DEFAULT
+constexpr int LB_TUNE_LIBRARY_DEFAULT = 0;
 
 const double W3[3] = {1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0};
 const double W2[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
@@ -89,6 +93,7 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
             a.dst.f[k] = pop_k(c, to, k);
         }
         a.flags = c->flags; a.sb = c->sb;
+        a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
         a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2); a.uz = mom_k(c, 3);
         a.W = g.nx; a.H = g.ny; a.D = g.nz; a.dev = 0; a.ndev = 1;
         a.w0 = (float)W3[0]; a.w1 = (float)W3[1]; a.w7 = (float)W3[2];
@@ -105,6 +110,7 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         a.dst.f[k] = pop_k(c, to, k);
     }
     a.flags = c->flags; a.sb = c->sb;
+    a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
     a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2);
     a.psi = c->sc; a.ueq_x = c->sc + c->stride; a.ueq_y = c->sc + 2 * c->stride;
     a.W = g.nx; a.H = g.ny; a.dev = 0; a.ndev = 1;
@@ -224,6 +230,7 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     c->cfg = *cfg;
     if (c->cfg.graph_steps <= 0) c->cfg.graph_steps = 64;
     c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
+    c->tune = (cfg->tuning & LB_TUNE_EXPLICIT) ? (cfg->tuning & 0xff) : LB_TUNE_LIBRARY_DEFAULT;
     c->Q = cfg->lattice;
     c->N = N;
     c->stride = (N + 63) / 64 * 64;  // each population array starts on a 256-byte boundary

@@ -30,8 +30,9 @@ struct Nbr2 {
 // ---------------------------------------------------------------------------
 template <int MODE, bool MOM, bool PLOT, bool SC>
 __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
+    const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
     if (x >= a.W) return;
     const int o = x + a.W * y;
     const uint8_t fl = a.flags[o];

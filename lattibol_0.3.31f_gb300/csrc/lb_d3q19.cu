@@ -46,8 +46,12 @@ struct Nbr3 {
 // ---------------------------------------------------------------------------
 template <int MODE, bool MOM, bool PLOT>
 __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
+    // blocks are dispatched in linear order; a reversed step maps them to the
+    // lattice back to front so it begins where the previous step ended
+    const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
+    const int z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
     if (x >= a.W) return;
     const int o = x + a.W * (y + a.H * z);
     const uint8_t fl = a.flags[o];

@@ -20,6 +20,7 @@ struct D3Args {
     float *ux, *uy, *uz, *rho;
     float4 *plot;
     int W, H, D, dev, ndev;
+    int reverse;            // sweep the blocks in reverse order (L2 reuse across steps)
     float w0, w1, w7, tau_inv, ux_in, rho_out, Fx, Fy, Fz;
     float corr[19];         // moving-wall momentum term per direction
 };
@@ -33,6 +34,7 @@ struct D2Args {
     float4 *plot;
     float *psi, *ueq_x, *ueq_y;
     int W, H, dev, ndev;
+    int reverse;
     float w0, w1, w5, tau_inv, ux_in, rho_out, Fx, Fy, G, Gads;
     int psi_form;
     float corr[9];

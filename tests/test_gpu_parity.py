@@ -190,9 +190,11 @@ def _channel_flags(W, H, D, sphere=None, lid=False):
     return fl.reshape(-1)
 
 
-def test_context_native_d3q19_vs_oracle(pkg, oracle):
+@pytest.mark.parametrize("tuning", [0x100, 0x101], ids=["forward", "alternating"])
+def test_context_native_d3q19_vs_oracle(pkg, oracle, tuning):
     """cfg2's physics on a small box: x-periodic channel, half-way bounce-back
-    walls in y/z, a sphere, body force, a moving wall, 40 steps, bit-exact."""
+    walls in y/z, a sphere, body force, a moving wall, 40 steps, bit-exact
+    (with and without the alternating sweep order)."""
     W, H, D = 64, 24, 20
     N = W * H * D
     flags = _channel_flags(W, H, D, sphere=(20, 12, 10, 5), lid=True)
@@ -205,7 +207,7 @@ def test_context_native_d3q19_vs_oracle(pkg, oracle):
     tau_inv = np.float32(1 / 0.55)
     F = (np.float32(1e-6), np.float32(2e-7), np.float32(0))
     lat = pkg.Lattice(19, W, H, D, tau_inv=tau_inv, force=F, wall_u=(0.04, 0.0, 0.01),
-                      graph_steps=8)
+                      graph_steps=8, tuning=tuning)
     lat.set_flags(flags)
     f0 = oracle.d3q19_equilibrium(rho, ux, uy, z, *w)
     lat.set_populations(f0)
@@ -265,7 +267,8 @@ def test_context_lid_cavity_d2q9_vs_oracle(pkg, oracle):
     fl[0, :] = 3  # row 0 is the top (physical +y = row-1)
     fl = fl.reshape(-1)
     tau_inv = np.float32(1 / 0.6)
-    lat = pkg.Lattice(9, W, H, tau_inv=tau_inv, wall_u=(0.1, 0, 0), graph_steps=16)
+    lat = pkg.Lattice(9, W, H, tau_inv=tau_inv, wall_u=(0.1, 0, 0), graph_steps=16,
+                      tuning=0x101)
     lat.set_flags(fl)
     lat.init_equilibrium()
     f = oracle.d2q9_equilibrium(np.ones(N, np.float32), np.zeros(N, np.float32),
