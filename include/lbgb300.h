@@ -95,6 +95,18 @@ int lb_abi_release_d3q19(DataD3Q19 *data);
  * energy, max|u|, n_fluid}.  Blocks the calling thread until done. */
 int lb_reduce_d2q9(const DataD2Q9 *data, double out[7]);
 int lb_reduce_d3q19(const DataD3Q19 *data, double out[7]);
+/* No counterpart in the reference.  The sums of lb_reduce_d3q19 for callers
+ * that cannot allocate device memory (a host whose GPU memory all belongs to
+ * its own pool allocator, or a real-time loop in which cudaMalloc/cudaFree
+ * could synchronise the device).  It calls no allocator: its scratch is a
+ * fixed 128 KiB array in the library's device memory, which every GPU that
+ * loads the library keeps until the process exits.  Lattices of more than
+ * 153 288 704 nodes are rejected with LB_ERR_ARG and a message in
+ * lb_abi_last_error().  The first call on a device looks up the array's
+ * device address (make it before any stream capture begins).  Calls share the
+ * array, so calls that overlap on the GPU race; results equal
+ * lb_reduce_d3q19's up to FP64 summation order. */
+int lb_reduce_d3q19_noalloc(const DataD3Q19 *data, double out[7]);
 /* The reference's per-step host sequence (SimulationD3Q19::runLBM, reference
  * src/simulation_d3q19.cu:350-430, without the GL map/unmap and the extra
  * device-wide synchronisations): for each step streaming_d3q19,

@@ -107,6 +107,7 @@ PROTOTYPES = [
     ("lb_abi_release_d3q19", _c.c_int, [_c.POINTER(DataD3Q19)]),
     ("lb_reduce_d2q9", _c.c_int, [_c.POINTER(DataD2Q9), _c.POINTER(_c.c_double)]),
     ("lb_reduce_d3q19", _c.c_int, [_c.POINTER(DataD3Q19), _c.POINTER(_c.c_double)]),
+    ("lb_reduce_d3q19_noalloc", _c.c_int, [_c.POINTER(DataD3Q19), _c.POINTER(_c.c_double)]),
     ("lb_run_lbm_d3q19", _c.c_int, [_c.POINTER(DataD3Q19), _c.c_void_p,
                                     _c.POINTER(lb_run_params_d3q19), _c.c_int, _c.c_void_p]),
     ("lb_abi_last_error", _c.c_char_p, []),

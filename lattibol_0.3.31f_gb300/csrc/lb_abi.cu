@@ -120,6 +120,8 @@ bool bad_d2(const DataD2Q9 *d, const char *where) {
 
 }  // namespace
 
+void lb::abi_record_error(const char *where, const char *what) { set_err(where, what); }
+
 extern "C" {
 
 int lb_abi_set_mode(int mode) {

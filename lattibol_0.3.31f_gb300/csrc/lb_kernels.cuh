@@ -77,5 +77,14 @@ int reduce_partials_size();
 cudaError_t launch_reduce(const float *rho, const float *ux, const float *uy, const float *uz,
                           const uint8_t *solid, uint8_t mask, long N, double *partials,
                           double *out_dev, cudaStream_t s);
+// the same two passes with a caller-chosen number of first-pass blocks
+// (partials must hold 7 * nblocks doubles)
+cudaError_t launch_reduce_blocks(const float *rho, const float *ux, const float *uy,
+                                 const float *uz, const uint8_t *solid, uint8_t mask, long N,
+                                 int nblocks, double *partials, double *out_dev,
+                                 cudaStream_t s);
+
+// records a message for lb_abi_last_error() on the calling thread
+void abi_record_error(const char *where, const char *what);
 
 }  // namespace lb

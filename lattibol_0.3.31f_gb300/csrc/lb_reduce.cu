@@ -107,4 +107,16 @@ cudaError_t launch_reduce(const float *rho, const float *ux, const float *uy, co
     return cudaGetLastError();
 }
 
+cudaError_t launch_reduce_blocks(const float *rho, const float *ux, const float *uy,
+                                 const float *uz, const uint8_t *solid, uint8_t mask, long N,
+                                 int nblocks, double *partials, double *out_dev,
+                                 cudaStream_t s) {
+    if (nblocks < 1) return cudaErrorInvalidValue;
+    reduce_pass1<<<nblocks, RED_THREADS, 0, s>>>(rho, ux, uy, uz, solid, mask, N, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce_pass2<<<1, RED_THREADS, 0, s>>>(partials, nblocks, out_dev);
+    return cudaGetLastError();
+}
+
 }  // namespace lb
