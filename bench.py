@@ -1,15 +1,18 @@
-"""Benchmark of the D3Q19 fused collide+stream hot path on one GB300.
+"""Benchmark of the lattice Boltzmann hot path on one GB300.
 
-Workload (the channel-flow-past-a-sphere case): D3Q19, 256x128x128 nodes,
-FP32 populations, tau = 0.55, x-periodic, uniform body force gx = 1e-6,
-half-way bounce-back walls on the y and z faces, a voxelised sphere of radius
-16 centred at (64, 64, 64), equilibrium initialisation at rho = 1.  A step is
-one lattice time step over all nodes; the metric is GLUPS (lattice node
-updates per second, all nodes counted, as the reference counts MLUPS in
-src/output.cpp:172).  The population state (1.28 GB for two sets) is larger
-than L2, so every step streams from HBM.
+Default workload ("channel", the headline): D3Q19 channel flow past a sphere,
+256x128x128 nodes, FP32 populations, tau = 0.55, x-periodic, uniform body
+force gx = 1e-6, half-way bounce-back walls on the y and z faces, a voxelised
+sphere of radius 16 centred at (64, 64, 64), equilibrium initialisation at
+rho = 1.  A step is one lattice time step over all nodes; the metric is GLUPS
+(lattice node updates per second, all nodes counted, as the reference counts
+MLUPS in src/output.cpp:172).  The population state (1.28 GB for two sets)
+is larger than L2, so every step streams from HBM.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Other workloads (--workload) measure the remaining configurations with the
+same JSON line: "cavity" (D2Q9 lid-driven cavity 256x256, tau 0.6, lid 0.1).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
 --impl reference times the reference algorithm on the host cores instead
 (the OpenMP C restatement in oracle/, run with all host threads on the same
@@ -17,7 +20,6 @@ lattice): the reference itself is a CUDA/Qt desktop application with no CPU
 path, and its kernels cannot be built on the GPU machine.
 """
 import argparse
-import ctypes
 import json
 import os
 import statistics
@@ -30,29 +32,89 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NX, NY, NZ = 256, 128, 128
-TAU = 0.55
-GX = 1e-6
-SPHERE = (64, 64, 64, 16)
-# algorithmic bytes per lattice update of the fused kernel: 19 loads + 19
-# stores of 4 bytes + 1 flag byte (moments are written on the last step only)
-BYTES_PER_LU = 2 * 19 * 4 + 1
-# DRAM bytes per launch of the fused kernel (dram__bytes_read.sum +
-# dram__bytes_write.sum) from the ncu capture summarised in
-# profiles/d3q19_fused_channel_256x128x128.md (captured at 128^3 and scaled
-# by the node count to this lattice)
-NCU_TRAFFIC_PER_LAUNCH = 522.1e6
 FALLBACK_HBM_GBS = 6800.0
 
 
-def channel_flags():
-    fl = np.zeros((NZ, NY, NX), np.uint8)
-    fl[:, 0, :] = fl[:, -1, :] = 1
-    fl[0, :, :] = fl[-1, :, :] = 1
-    cx, cy, cz, r = SPHERE
-    z, y, x = np.ogrid[0:NZ, 0:NY, 0:NX]
-    fl[(x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 <= r * r] = 1
-    return fl.reshape(-1)
+class Workload:
+    """One benchmark configuration: lattice, extents, physics, and the
+    algorithmic bytes per lattice update of the kernel it times."""
+
+    def __init__(self, name, lattice, size, tau, steps, bytes_per_lu, force=(0, 0, 0),
+                 wall_u=(0, 0, 0), traffic=None, profile=None, describe=None, G=0.0,
+                 storage=0, rho_ref=0.0, dtype="f32"):
+        self.name, self.lattice, self.size, self.tau = name, lattice, tuple(size), tau
+        self.steps, self.bytes_per_lu, self.force, self.wall_u = steps, bytes_per_lu, force, wall_u
+        self.traffic, self.profile, self.describe = traffic, profile, describe or {}
+        self.G, self.storage, self.rho_ref, self.dtype = G, storage, rho_ref, dtype
+
+    def initial_rho(self):
+        """None (uniform rho = 1) or the seeded spinodal density field
+        rho = 0.693 (1 + eps), eps ~ U[-0.01, 0.01] (numpy PCG64, seed 2024)."""
+        if not self.name.startswith("spinodal"):
+            return None
+        rng = np.random.default_rng(2024)
+        return (0.693 * (1 + rng.uniform(-0.01, 0.01, self.N))).astype(np.float32)
+
+    @property
+    def N(self):
+        return int(np.prod(self.size))
+
+    def flags(self):
+        nx, ny, nz = self.size
+        if self.name == "channel":
+            fl = np.zeros((nz, ny, nx), np.uint8)
+            fl[:, 0, :] = fl[:, -1, :] = 1
+            fl[0, :, :] = fl[-1, :, :] = 1
+            cx, cy, cz, r = 64, 64, 64, 16
+            z, y, x = np.ogrid[0:nz, 0:ny, 0:nx]
+            fl[(x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 <= r * r] = 1
+            return fl.reshape(-1)
+        if self.name == "cavity":
+            fl = np.zeros((ny, nx), np.uint8)
+            fl[:, 0] = fl[:, -1] = fl[-1, :] = 1
+            fl[0, :] = 3  # row 0 is the top wall (physical +y is row-1), moving with the lid
+            return fl.reshape(-1)
+        if self.name.startswith("spinodal"):
+            return np.zeros(self.N, np.uint8)  # fully periodic
+        raise ValueError(self.name)
+
+    def config(self, n_gpus):
+        c = {"workload": "%s_%s" % (self.name, "x".join(str(s) for s in self.size if s > 1)),
+             "lattice": "D3Q19" if self.lattice == 19 else "D2Q9", "nodes": list(self.size),
+             "tau": self.tau, "parallelism": "replicas" if n_gpus > 1 else "single"}
+        c.update(self.describe)
+        return c
+
+
+WORKLOADS = {
+    # 19x4 loads + 19x4 stores + 1 flag byte (moments only on the last step)
+    "channel": Workload(
+        "channel", 19, (256, 128, 128), 0.55, 20000, 2 * 19 * 4 + 1, force=(1e-6, 0, 0),
+        # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+        # the ncu capture in profiles/d3q19_fused_channel_256x128x128.md (captured at
+        # 128^3 and scaled by the node count to this lattice)
+        traffic=522.1e6, profile="profiles/d3q19_fused_channel_256x128x128.md",
+        describe={"body_force_x": 1e-6, "sphere": {"center": [64, 64, 64], "radius": 16},
+                  "boundaries": "x periodic, half-way bounce-back on y/z faces and sphere",
+                  "init": "equilibrium rho=1 u=0",
+                  "l2": "state (1.28 GB) larger than L2"}),
+    "cavity": Workload(
+        "cavity", 9, (256, 256, 1), 0.6, 10000, 2 * 9 * 4 + 1, wall_u=(0.1, 0, 0),
+        describe={"lid_velocity": 0.1, "boundaries": "half-way bounce-back box, moving top wall",
+                  "init": "equilibrium rho=1 u=0",
+                  "l2": "state (4.7 MB) fits L2: launch-latency bound, graph-replayed"}),
+}
+# D3Q19 Shan-Chen spinodal decomposition, 256^3 periodic, tau = 1, G = -5,
+# psi = 1 - exp(-rho); algorithmic bytes/LU: populations read + written once,
+# psi written and read once: 153 + 8 (FP32), 77 + 8 (16-bit deviation storage)
+for _st, _nm, _b in [(0, "f32", 161), (1, "f16", 85), (2, "bf16", 85)]:
+    WORKLOADS["spinodal" + ("" if _st == 0 else "_" + _nm)] = Workload(
+        "spinodal" + ("" if _st == 0 else "_" + _nm), 19, (256, 256, 256), 1.0, 10000, _b,
+        G=-5.0, storage=_st, rho_ref=0.693, dtype=_nm,
+        describe={"G": -5.0, "psi": "1-exp(-rho)", "storage": _nm,
+                  "storage_offset": "f_k - w_k*0.693" if _st else None,
+                  "init": "rho=0.693(1+eps), eps~U[-0.01,0.01], seed 2024, u=0",
+                  "boundaries": "periodic", "l2": "state larger than L2"})
 
 
 def measured_peak():
@@ -73,6 +135,7 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -86,7 +149,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.out = ""
         if self.proc:
             time.sleep(0.25)
             self.proc.terminate()
@@ -141,56 +203,61 @@ def dist_max(dist, v):
     return float(t.item())
 
 
-def cpu_baseline(budget_s=15.0, max_steps=None):
-    """The oracle's float port of the reference loop, native mode, on the full
-    lattice with all host threads, timed for a bounded number of steps."""
+def cpu_baseline(wl, budget_s=15.0, max_steps=None):
+    """The oracle's float port of the reference loop (swap streaming + collision,
+    native boundary mode) on the workload's full lattice with all host threads,
+    timed for a bounded number of steps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import lb_oracle as orc
     orc.lib()
-    N = NX * NY * NZ
-    flags = channel_flags()
+    N = wl.N
+    nx, ny, nz = wl.size
+    flags = wl.flags()
     one = np.ones(N, np.float32)
     z = np.zeros(N, np.float32)
-    w = (np.float32(12 / 36), np.float32(2 / 36), np.float32(1 / 36))
-    f = orc.d3q19_equilibrium(one, z, z, z, *w)
-    corr = np.zeros(19, np.float32)
-    tau_inv = np.float32(1 / TAU)
-    F = (np.float32(GX), np.float32(0), np.float32(0))
+    tau_inv = np.float32(1 / wl.tau)
+    F = tuple(np.float32(v) for v in wl.force)
+    rho0 = wl.initial_rho()
+    if rho0 is not None:
+        one = rho0
+    psi = np.zeros(N, np.float32) if wl.G != 0 else None
+    if wl.lattice == 19:
+        w = (np.float32(12 / 36), np.float32(2 / 36), np.float32(1 / 36))
+        f = orc.d3q19_equilibrium(one, z, z, z, *w)
+    else:
+        w = (np.float32(16 / 36), np.float32(4 / 36), np.float32(1 / 36))
+        f = orc.d2q9_equilibrium(one, z, z, *w)
+    corr = orc.wall_correction(wl.lattice, wl.wall_u)
     steps = 0
     t0 = time.perf_counter()
     while True:
-        orc.d3q19_stream_native(f, flags, corr, NX, NY, NZ)
-        orc.d3q19_collide_native(f, flags, None, NX, NY, NZ, *w, tau_inv, F)
+        if wl.lattice == 19:
+            orc.d3q19_stream_native(f, flags, corr, nx, ny, nz)
+            orc.d3q19_collide_native(f, flags, None, nx, ny, nz, *w, tau_inv, F, G=wl.G, psi=psi)
+        else:
+            orc.d2q9_stream_native(f, flags, corr, nx, ny)
+            orc.d2q9_collide_native(f, flags, None, nx, ny, *w, tau_inv, F[:2])
         steps += 1
         el = time.perf_counter() - t0
         if el >= budget_s or (max_steps and steps >= max_steps):
             break
     return {"value": N * steps / el / 1e9, "unit": "GLUPS", "cores": orc.num_threads(),
             "kind": "port", "steps": steps, "seconds": el,
-            "sample": "%d time steps of the full %dx%dx%d lattice (oracle/lb_oracle.c, float, "
-                      "OpenMP)" % (steps, NX, NY, NZ)}
+            "sample": "%d time steps of the full %s lattice (oracle/lb_oracle.c, float, OpenMP)"
+                      % (steps, "x".join(str(s) for s in wl.size if s > 1))}
 
 
-def config_block(n_gpus):
-    return {"workload": "d3q19_channel_sphere_256x128x128", "lattice": "D3Q19",
-            "nodes": [NX, NY, NZ], "tau": TAU, "body_force_x": GX,
-            "sphere": {"center": SPHERE[:3], "radius": SPHERE[3]},
-            "boundaries": "x periodic, half-way bounce-back on y/z faces and sphere",
-            "init": "equilibrium rho=1 u=0", "l2": "state (1.28 GB) larger than L2",
-            "parallelism": "replicas" if n_gpus > 1 else "single"}
-
-
-def run_reference(args):
+def run_reference(args, wl):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     budget = float(os.environ.get("LB_CPU_BUDGET_S", "60"))
-    cb = cpu_baseline(budget_s=budget, max_steps=args.steps)
+    cb = cpu_baseline(wl, budget_s=budget, max_steps=args.steps)
     line = {"impl": "reference", "metric": "GLUPS", "value": cb["value"], "unit": "GLUPS",
             "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 0,
             "ms_per_step": 1e3 * cb["seconds"] / cb["steps"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_block(1),
+            "config": wl.config(1),
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "GLUPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -201,21 +268,26 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="channel", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--tuning", type=lambda v: int(v, 0), default=0,
                     help="lb_config.tuning (0 = the library's default)")
+    ap.add_argument("--graph-steps", type=int, default=64)
     ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
     if args.size:
-        global NX, NY, NZ
-        NX, NY, NZ = args.size
+        wl.size = tuple(args.size)
+        wl.traffic = None
+    if args.steps is None:
+        args.steps = wl.steps
     if args.impl == "reference":
-        return run_reference(args)
+        return run_reference(args, wl)
     args.warmup = max(args.warmup, 3)
 
     ws, rank, local = dist_env()
@@ -223,14 +295,17 @@ def main():
     import __graft_entry__ as ge
     pkg = ge.load_package()
     L = pkg.lib()
-    N = NX * NY * NZ
-    flags = channel_flags()
+    N = wl.N
+    nx, ny, nz = wl.size
+    flags = wl.flags()
 
     # ------------------------------------------------ device-resident throughput
-    lat = pkg.Lattice(19, NX, NY, NZ, tau_inv=np.float32(1 / TAU),
-                      force=(np.float32(GX), 0, 0), graph_steps=64, tuning=args.tuning)
+    lat = pkg.Lattice(wl.lattice, nx, ny, nz, tau_inv=np.float32(1 / wl.tau),
+                      force=tuple(np.float32(v) for v in wl.force), wall_u=wl.wall_u,
+                      graph_steps=args.graph_steps, tuning=args.tuning, G=wl.G,
+                      storage=wl.storage, rho_ref=wl.rho_ref)
     lat.set_flags(flags)
-    lat.init_equilibrium()
+    lat.init_equilibrium(wl.initial_rho())
     lat.step(args.warmup)
     lat.synchronize()
     if dist:
@@ -241,48 +316,51 @@ def main():
     launches = lat.launches() - n0
     ms = dist_max(dist, ms)
     glups = ws * N * args.steps / (ms * 1e-3) / 1e9
-    rho, ux, uy, uz = lat.moments()
-    assert np.isfinite(rho).all() and np.isfinite(ux).all()
+    mom = lat.moments()
+    assert np.isfinite(mom[0]).all() and np.isfinite(mom[1]).all()
     lat.close()
 
     # ------------------------------------------------ end to end through the C ABI
-    # the reference's per-step host sequence (streaming_d3q19, collision_d3q19,
-    # read_value_3d, 16-byte probe copy) in fused mode, driven by the library's
-    # native host loop, with the initial state uploaded from pinned host memory
-    # and the final moment fields read back inside the timed region
     e2e = None
-    if args.e2e_steps > 0:
-        e2e = measure_e2e(pkg, L, flags, args.e2e_steps, ws, dist)
+    if args.e2e_steps > 0 and wl.name == "channel":
+        e2e = measure_e2e(pkg, L, wl, flags, args.e2e_steps, ws, dist)
 
     if rank != 0:
         return 0
     peak, peak_kind = measured_peak()
     kern_ms = ms / args.steps
-    achieved = BYTES_PER_LU * N / (kern_ms * 1e-3) / 1e9
+    achieved = wl.bytes_per_lu * N / (kern_ms * 1e-3) / 1e9
     line = {
         "metric": "GLUPS", "value": glups, "unit": "GLUPS", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": config_block(ws),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
+        "data": "synthetic", "config": wl.config(ws),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "bytes_per_lu": BYTES_PER_LU,
-                     "traffic": NCU_TRAFFIC_PER_LAUNCH},
+                     "bytes_per_lu": wl.bytes_per_lu, "traffic": wl.traffic},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline and ws == 1:
-        cb = cpu_baseline(budget_s=float(os.environ.get("LB_CPU_BUDGET_S", "12")))
+        cb = cpu_baseline(wl, budget_s=float(os.environ.get("LB_CPU_BUDGET_S", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     return 0
 
 
-def measure_e2e(pkg, L, flags, steps, ws, dist):
+def measure_e2e(pkg, L, wl, flags, steps, ws, dist):
+    """The reference's per-step host sequence (streaming_d3q19,
+    collision_d3q19 with moments and plot, read_value_3d, 16-byte probe copy)
+    through the drop-in entry points in fused mode, driven by the library's
+    native host loop lb_run_lbm_d3q19; the initial populations and walls are
+    uploaded from pinned host memory and the final moment fields read back
+    inside the timed region.  Reference semantics (Zou-He x faces, walls
+    stored full-way) on the same lattice and walls."""
     import ctypes as C
-    N = NX * NY * NZ
+    N = wl.N
+    nx, ny, nz = wl.size
     pinned_ptrs = []
 
     def pinned(shape, dtype):
@@ -304,10 +382,10 @@ def measure_e2e(pkg, L, flags, steps, ws, dist):
     sb = pinned((N,), np.uint8)
     sb[:] = 0
     out_fields = [pinned((N,), np.float32) for _ in range(4)]
-    dd = pkg.DeviceData(19, NX, NY, NZ)
+    dd = pkg.DeviceData(19, nx, ny, nz)
     assert L.lb_abi_set_mode(pkg.abi.LB_ABI_FUSED) == 0
-    params = pkg.abi.lb_run_params_d3q19(w[0], w[1], w[2], np.float32(1 / TAU), 0.0, 0.0, 0.0,
-                                         1.0, (C.c_int * 3)(NX // 2, NY // 2, NZ // 2))
+    params = pkg.abi.lb_run_params_d3q19(w[0], w[1], w[2], np.float32(1 / wl.tau), 0.0, 0.0,
+                                         0.0, 1.0, (C.c_int * 3)(nx // 2, ny // 2, nz // 2))
     value = np.zeros(4, np.float32)
     # warm-up (allocates the library's second population set)
     dd.upload(f_host)

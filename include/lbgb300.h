@@ -180,6 +180,7 @@ typedef struct {
     int psi_form;       /* LB_PSI_* */
     int graph_steps;    /* steps per captured CUDA graph in lb_step (0 = default 64) */
     int tuning;         /* LB_TUNE_* bits; LB_TUNE_DEFAULT picks the measured best */
+    float rho_ref;      /* 16-bit storage keeps f_k - w_k*rho_ref (0 = 1.0) */
 } lb_config;
 
 typedef struct lb_ctx lb_ctx;

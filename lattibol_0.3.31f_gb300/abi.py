@@ -65,7 +65,7 @@ class lb_config(ctypes.Structure):
                 ("u_in", ctypes.c_float * 3), ("rho_out", ctypes.c_float),
                 ("wall_u", ctypes.c_float * 3), ("G", ctypes.c_float), ("G_ads", ctypes.c_float),
                 ("psi_form", ctypes.c_int), ("graph_steps", ctypes.c_int),
-                ("tuning", ctypes.c_int)]
+                ("tuning", ctypes.c_int), ("rho_ref", ctypes.c_float)]
 
 
 class lb_run_params_d3q19(ctypes.Structure):

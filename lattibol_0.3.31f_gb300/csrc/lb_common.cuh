@@ -8,6 +8,8 @@
 // float arithmetic, which is what the parity tests check.
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -79,6 +81,35 @@ __device__ __forceinline__ int wrap_add(int v, int c, int n) {
 
 // streaming loads: read-only for the kernel's lifetime, touched once per step
 __device__ __forceinline__ float ld_stream(const float *p) { return __ldg(p); }
+
+// Population storage.  FP32 stores f_k itself.  The 16-bit forms store the
+// deviation f_k - wr_k from an offset wr_k = w_k * rho_ref (rounded to float
+// once on the host); the arithmetic stays FP32: load = wr_k + widen(h),
+// store = narrow_rne(f_k - wr_k).
+template <typename S> struct Store;
+template <> struct Store<float> {
+    static constexpr int kind = 0;
+    __device__ __forceinline__ static float load(const float *p, float) { return __ldg(p); }
+    __device__ __forceinline__ static void store(float *p, float v, float) { *p = v; }
+};
+template <> struct Store<__half> {
+    static constexpr int kind = 1;
+    __device__ __forceinline__ static float load(const __half *p, float wr) {
+        return wr + __half2float(__ldg(p));
+    }
+    __device__ __forceinline__ static void store(__half *p, float v, float wr) {
+        *p = __float2half_rn(v - wr);
+    }
+};
+template <> struct Store<__nv_bfloat16> {
+    static constexpr int kind = 2;
+    __device__ __forceinline__ static float load(const __nv_bfloat16 *p, float wr) {
+        return wr + __bfloat162float(__ldg(p));
+    }
+    __device__ __forceinline__ static void store(__nv_bfloat16 *p, float v, float wr) {
+        *p = __float2bfloat16_rn(v - wr);
+    }
+};
 
 // ---------------------------------------------------------------- BGK, D3Q19
 // relaxation towards the equilibrium at velocity (ux,uy,uz), reference

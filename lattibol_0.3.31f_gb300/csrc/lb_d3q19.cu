@@ -1,12 +1,14 @@
 // lb_d3q19.cu -- D3Q19 kernels: the fused pull-stream + collide step (the hot
-// path), and the reference-exact standalone streaming / collision / border
-// kernels behind the drop-in entry points.
+// path) with FP32 or 16-bit deviation storage and an optional Shan-Chen
+// force, the density (psi) pass of the Shan-Chen step, and the
+// reference-exact standalone streaming / collision / border kernels behind
+// the drop-in entry points.
 //
-// Layout: structure of arrays, one float array per population, node index
+// Layout: structure of arrays, one array per population, node index
 // o = x + W*(y + H*z) (reference src/streaming.cu:98).  A thread owns one
 // node; a block covers a run of x at fixed (y, z), so every population load
-// and store of a warp is one coalesced 128-byte row (shifted by one element
-// for populations with c_x != 0).
+// and store of a warp is one coalesced row (shifted by one element for
+// populations with c_x != 0).
 #include "lb_kernels.cuh"
 
 namespace lb {
@@ -30,10 +32,46 @@ struct Nbr3 {
     }
 };
 
+// block -> lattice coordinates; a reversed step maps the linearly dispatched
+// blocks back to front so that it begins where the previous step ended
+struct Coord3 {
+    int x, y, z;
+    __device__ __forceinline__ Coord3(const D3Args &a) {
+        const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+        x = bx * blockDim.x + threadIdx.x;
+        y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
+        z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    }
+};
+
+// Native pull of the 19 populations of fluid node o (see d3q19_fused_kernel).
+template <typename S>
+__device__ __forceinline__ void pull_native(const D3Args &a, int o, const Nbr3 &n, uint8_t fl,
+                                            float (&g)[19]) {
+    const S *const *src = (const S *const *)(a.src.f);  // storage arrays behind float*
+    if (fl & CELL_NEAR_WALL) {
+#pragma unroll
+        for (int k = 0; k < 19; k++) {
+            const int up = o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k));
+            const uint8_t fu = k == 0 ? 0 : a.flags[up];
+            if (fu & CELL_WALL) {
+                const float v = Store<S>::load(src[d3_opp(k)] + o, a.wr[d3_opp(k)]);
+                g[k] = (fu & CELL_MOVING) ? v - a.corr[d3_opp(k)] : v;
+            } else {
+                g[k] = Store<S>::load(src[k] + up, a.wr[k]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 19; k++)
+            g[k] = Store<S>::load(src[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)), a.wr[k]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Fused step.  Pull: population k of node o comes from o - c_k.
 //  * fluid node: pull all 18, (reference mode) Zou-He on the x faces,
-//    moments, (native) force shift, BGK, store to dst at o.
+//    moments, (native) force shift and Shan-Chen shift, BGK, store to dst.
 //  * reference mode, solid node: reproduces the reference's full-way
 //    bounce-back storage.  Slot m of a solid node receives, by the swap
 //    streaming of src/streaming.cu, the population opp(m) leaving
@@ -43,15 +81,14 @@ struct Nbr3 {
 //  * native mode: a fluid node whose upstream neighbour is a wall takes its
 //    own outgoing opposite population (half-way bounce-back), minus the
 //    moving-wall term corr[opp(k)].  Wall nodes are not updated.
+// Shan-Chen (native): F = -G psi(x) sum_k w_k psi(x + c_k) c_k with psi from
+// the density pass of this step, applied as a velocity shift F/(tau_inv rho)
+// like the reference's force (src/collision.cu:92-96).
 // ---------------------------------------------------------------------------
-template <int MODE, bool MOM, bool PLOT>
+template <int MODE, bool MOM, bool PLOT, typename S, bool SC>
 __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
-    // blocks are dispatched in linear order; a reversed step maps them to the
-    // lattice back to front so it begins where the previous step ended
-    const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
-    const int x = bx * blockDim.x + threadIdx.x;
-    const int y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
-    const int z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const Coord3 c(a);
+    const int x = c.x, y = c.y, z = c.z;
     if (x >= a.W) return;
     const int o = x + a.W * (y + a.H * z);
     const uint8_t fl = a.flags[o];
@@ -81,25 +118,12 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
     }
 
     float g[19];
-    if (MODE == MODE_NATIVE && (fl & CELL_NEAR_WALL)) {
-#pragma unroll
-        for (int k = 0; k < 19; k++) {
-            const int up = o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k));
-            const uint8_t fu = k == 0 ? 0 : a.flags[up];
-            if (fu & CELL_WALL) {
-                const float v = ld_stream(a.src.f[d3_opp(k)] + o);
-                g[k] = (fu & CELL_MOVING) ? v - a.corr[d3_opp(k)] : v;
-            } else {
-                g[k] = ld_stream(a.src.f[k] + up);
-            }
-        }
+    if (MODE == MODE_NATIVE) {
+        pull_native<S>(a, o, n, fl, g);
     } else {
 #pragma unroll
         for (int k = 0; k < 19; k++)
             g[k] = ld_stream(a.src.f[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)));
-    }
-
-    if (MODE == MODE_REF) {
         if (x == 0 && a.dev == 0)
             d3q19_zou_he_west(g, a.ux_in);
         else if (x == a.W - 1 && a.dev == a.ndev - 1)
@@ -115,10 +139,47 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
         if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
         if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
         if (a.Fz != 0.f) ez = uz + a.Fz / (rho * a.tau_inv);
+        if (SC) {
+            float IFx = 0.f, IFy = 0.f, IFz = 0.f;
+#pragma unroll
+            for (int k = 1; k < 19; k++) {
+                const float t = (k < 7 ? a.w1 : a.w7) *
+                                __ldg(a.psi + o + n.off(d3_cx(k), d3_cy(k), d3_cz(k)));
+                if (d3_cx(k) > 0) IFx = IFx + t; else if (d3_cx(k) < 0) IFx = IFx - t;
+                if (d3_cy(k) > 0) IFy = IFy + t; else if (d3_cy(k) < 0) IFy = IFy - t;
+                if (d3_cz(k) > 0) IFz = IFz + t; else if (d3_cz(k) < 0) IFz = IFz - t;
+            }
+            const float gp = -a.G * a.psi[o];
+            ex = ex + (gp * IFx) / (a.tau_inv * rho);
+            ey = ey + (gp * IFy) / (a.tau_inv * rho);
+            ez = ez + (gp * IFz) / (a.tau_inv * rho);
+        }
     }
     d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+    S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
-    for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+    for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], a.wr[k]);
+}
+
+// Density pass of the Shan-Chen step: psi(rho) of the post-stream density of
+// every fluid node (the sum in the order of the collision's moments, so rho
+// is the same float the fused kernel computes), 0 at walls.
+template <typename S>
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a) {
+    const Coord3 c(a);
+    if (c.x >= a.W) return;
+    const int o = c.x + a.W * (c.y + a.H * c.z);
+    const uint8_t fl = a.flags[o];
+    if (fl & CELL_WALL) {
+        a.psi[o] = 0.f;
+        return;
+    }
+    const Nbr3 n(c.x, c.y, c.z, a.W, a.H, a.D);
+    float g[19];
+    pull_native<S>(a, o, n, fl, g);
+    const float rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8] + g[9] +
+                      g[10] + g[11] + g[12] + g[13] + g[14] + g[15] + g[16] + g[17] + g[18];
+    a.psi[o] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
 // ---------------------------------------------------------------------------
@@ -215,6 +276,56 @@ __global__ void d3q19_equilibrium_kernel(Pop<19> p, const float *rho, const floa
     for (int k = 0; k < 19; k++) p.f[k][o] = g[k];
 }
 
+struct Wr19 {
+    float v[19];
+};
+
+// the same equilibrium, stored in 16-bit deviation form
+template <typename S>
+__global__ void d3q19_equilibrium_store_kernel(Pop<19> p, const float *rho, const float *ux,
+                                               const float *uy, const float *uz, int N,
+                                               float w0, float w1, float w7, Wr19 wr) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= N) return;
+    float g[19];
+#pragma unroll
+    for (int k = 0; k < 19; k++) g[k] = 0.f;
+    d3q19_bgk(g, ux ? ux[o] : 0.f, uy ? uy[o] : 0.f, uz ? uz[o] : 0.f, rho ? rho[o] : 1.f, w0,
+              w1, w7, 1.f);
+    S *const *dst = reinterpret_cast<S *const *>(p.f);
+#pragma unroll
+    for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], wr.v[k]);
+}
+
+cudaError_t launch_d3q19_equilibrium_storage(const Pop<19> &p, const float *rho, const float *ux,
+                                             const float *uy, const float *uz, int N, float w0,
+                                             float w1, float w7, const float *wr, int storage,
+                                             cudaStream_t s) {
+    Wr19 w;
+    for (int k = 0; k < 19; k++) w.v[k] = wr[k];
+    const unsigned blocks = (unsigned)((N + 255) / 256);
+    if (storage == 1)
+        d3q19_equilibrium_store_kernel<__half><<<blocks, 256, 0, s>>>(p, rho, ux, uy, uz, N, w0,
+                                                                      w1, w7, w);
+    else if (storage == 2)
+        d3q19_equilibrium_store_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>(p, rho, ux, uy, uz,
+                                                                             N, w0, w1, w7, w);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+template <typename S>
+__global__ void to_storage_kernel(const float *src, S *dst, long n, float wr) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) Store<S>::store(dst + i, src[i], wr);
+}
+template <typename S>
+__global__ void from_storage_kernel(const S *src, float *dst, long n, float wr) {
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = Store<S>::load(src + i, wr);
+}
+
 // ---------------------------------------------------------------- launchers
 static dim3 grid_of(int W, int H, int D) { return dim3((W + D3_BLOCK - 1) / D3_BLOCK, H, D); }
 
@@ -222,7 +333,7 @@ cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, c
     const dim3 g = grid_of(a.W, a.H, a.D), b(D3_BLOCK);
 #define LB_D3_CASE(M, MO, PL)                                                    \
     if (mode == M && mom == MO && plot == PL) {                                  \
-        d3q19_fused_kernel<M, MO, PL><<<g, b, 0, s>>>(a);                       \
+        d3q19_fused_kernel<M, MO, PL, float, false><<<g, b, 0, s>>>(a);         \
         return cudaGetLastError();                                               \
     }
     LB_D3_CASE(MODE_REF, true, true)
@@ -230,9 +341,55 @@ cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, c
     LB_D3_CASE(MODE_REF, false, false)
     LB_D3_CASE(MODE_NATIVE, true, false)
     LB_D3_CASE(MODE_NATIVE, false, false)
-    LB_D3_CASE(MODE_NATIVE, true, true)
 #undef LB_D3_CASE
     return cudaErrorInvalidValue;
+}
+
+template <typename S>
+static cudaError_t native_launch(const D3Args &a, bool mom, bool sc, cudaStream_t s) {
+    const dim3 g = grid_of(a.W, a.H, a.D), b(D3_BLOCK);
+    if (sc) {
+        d3q19_density_kernel<S><<<g, b, 0, s>>>(a);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (mom) d3q19_fused_kernel<MODE_NATIVE, true, false, S, true><<<g, b, 0, s>>>(a);
+        else d3q19_fused_kernel<MODE_NATIVE, false, false, S, true><<<g, b, 0, s>>>(a);
+    } else {
+        if (mom) d3q19_fused_kernel<MODE_NATIVE, true, false, S, false><<<g, b, 0, s>>>(a);
+        else d3q19_fused_kernel<MODE_NATIVE, false, false, S, false><<<g, b, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc, cudaStream_t s) {
+    switch (storage) {
+    case 0: return native_launch<float>(a, mom, sc, s);
+    case 1: return native_launch<__half>(a, mom, sc, s);
+    case 2: return native_launch<__nv_bfloat16>(a, mom, sc, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_to_storage(const float *src, void *dst, long n, float wr, int storage,
+                              cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (storage == 1) to_storage_kernel<__half><<<blocks, 256, 0, s>>>(src, (__half *)dst, n, wr);
+    else if (storage == 2)
+        to_storage_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>(src, (__nv_bfloat16 *)dst, n, wr);
+    else to_storage_kernel<float><<<blocks, 256, 0, s>>>(src, (float *)dst, n, wr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_storage(const void *src, float *dst, long n, float wr, int storage,
+                                cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (storage == 1)
+        from_storage_kernel<__half><<<blocks, 256, 0, s>>>((const __half *)src, dst, n, wr);
+    else if (storage == 2)
+        from_storage_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)src,
+                                                                  dst, n, wr);
+    else from_storage_kernel<float><<<blocks, 256, 0, s>>>((const float *)src, dst, n, wr);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_d3q19_stream_swap(const Pop<19> &p, const uint8_t *sb, int W, int H, int D,

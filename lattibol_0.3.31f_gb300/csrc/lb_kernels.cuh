@@ -23,6 +23,10 @@ struct D3Args {
     int reverse;            // sweep the blocks in reverse order (L2 reuse across steps)
     float w0, w1, w7, tau_inv, ux_in, rho_out, Fx, Fy, Fz;
     float corr[19];         // moving-wall momentum term per direction
+    float wr[19];           // 16-bit storage: offsets w_k * rho_ref of the stored deviations
+    float *psi;             // Shan-Chen: pseudo-potential of the current step (density pass)
+    float G;                // Shan-Chen interaction strength
+    int psi_form;           // LB_PSI_REF or LB_PSI_EXP1
 };
 
 struct D2Args {
@@ -42,6 +46,20 @@ struct D2Args {
 
 // D3Q19
 cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, cudaStream_t s);
+// native mode with storage kind (0 f32, 1 f16, 2 bf16) and optional Shan-Chen
+// (sc: the density pass writing a.psi, then the fused step reading it)
+cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc, cudaStream_t s);
+// equilibrium written in 16-bit deviation storage (storage 1 or 2; Pop holds
+// the storage arrays reinterpreted as float*)
+cudaError_t launch_d3q19_equilibrium_storage(const Pop<19> &p, const float *rho, const float *ux,
+                                             const float *uy, const float *uz, int N, float w0,
+                                             float w1, float w7, const float *wr, int storage,
+                                             cudaStream_t s);
+// float <-> storage conversion of one population array (deviation from wr)
+cudaError_t launch_to_storage(const float *src, void *dst, long n, float wr, int storage,
+                              cudaStream_t s);
+cudaError_t launch_from_storage(const void *src, float *dst, long n, float wr, int storage,
+                                cudaStream_t s);
 cudaError_t launch_d3q19_stream_swap(const Pop<19> &p, const uint8_t *sb, int W, int H, int D,
                                      cudaStream_t s);
 cudaError_t launch_d3q19_collide(const D3Args &a, bool plot, cudaStream_t s);

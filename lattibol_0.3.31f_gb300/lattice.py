@@ -37,7 +37,7 @@ class Lattice:
     def __init__(self, lattice, nx, ny, nz=1, mode=abi.LB_MODE_NATIVE, tau_inv=1.0,
                  force=(0, 0, 0), u_in=(0, 0, 0), rho_out=1.0, wall_u=(0, 0, 0), G=0.0,
                  G_ads=0.0, psi_form=abi.LB_PSI_EXP1, graph_steps=64,
-                 storage=abi.LB_STORE_F32, tuning=abi.LB_TUNE_DEFAULT):
+                 storage=abi.LB_STORE_F32, tuning=abi.LB_TUNE_DEFAULT, rho_ref=0.0):
         L = _lib()
         cfg = abi.lb_config()
         L.lb_config_default(ctypes.byref(cfg), lattice, nx, ny, nz)
@@ -47,6 +47,7 @@ class Lattice:
             cfg.force[i], cfg.u_in[i], cfg.wall_u[i] = force[i], u_in[i], wall_u[i]
         cfg.G, cfg.G_ads, cfg.psi_form, cfg.graph_steps = G, G_ads, psi_form, graph_steps
         cfg.tuning = tuning
+        cfg.rho_ref = rho_ref
         self.cfg = cfg
         self.Q = lattice
         self.shape = (nx, ny, nz if lattice == 19 else 1)

@@ -227,6 +227,20 @@ void lbo_round_storage(float *f, long n, int kind)
         f[i] = kind == 1 ? lbo_f16_to_f32(lbo_f32_to_f16(f[i])) : lbo_bf16_to_f32(lbo_f32_to_bf16(f[i]));
 }
 
+void lbo_quantize_dev(float *f, int Q, long N, const float *wr, const uint8_t *flags, int kind)
+{
+#pragma omp parallel for schedule(static)
+    for (long o = 0; o < N; o++) {
+        if (flags && (flags[o] & LBO_SOLID)) continue;
+        for (int k = 0; k < Q; k++) {
+            const float d = f[(long)k * N + o] - wr[k];
+            const float q = kind == 1 ? lbo_f16_to_f32(lbo_f32_to_f16(d))
+                                      : lbo_bf16_to_f32(lbo_f32_to_bf16(d));
+            f[(long)k * N + o] = wr[k] + q;
+        }
+    }
+}
+
 int lbo_num_threads(void)
 {
 #ifdef _OPENMP

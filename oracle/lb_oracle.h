@@ -88,6 +88,10 @@ float lbo_f16_to_f32(uint16_t h);
 uint16_t lbo_f32_to_bf16(float v);
 float lbo_bf16_to_f32(uint16_t h);
 void lbo_round_storage(float *f, long n, int kind /* 1 = f16, 2 = bf16 */);
+/* emulate 16-bit deviation storage of a float population state: for every
+ * node with (flags == NULL || !(flags[o] & LBO_SOLID)) and every k,
+ * f[k][o] = wr[k] + widen(narrow_rne(f[k][o] - wr[k])), all in float */
+void lbo_quantize_dev(float *f, int Q, long N, const float *wr, const uint8_t *flags, int kind);
 
 int lbo_num_threads(void);
 void lbo_set_threads(int n);

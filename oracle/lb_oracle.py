@@ -214,6 +214,24 @@ def set_threads(n):
     lib().lbo_set_threads(int(n))
 
 
+def storage_offsets(lattice, rho_ref=1.0):
+    """wr_k = w_k * rho_ref, evaluated in double and rounded to float."""
+    w = D3_W if lattice == 19 else D2_W
+    r = float(np.float32(rho_ref))
+    return np.array([np.float32(wk * r) for wk in w], np.float32)
+
+
+def quantize_dev(f, wr, flags=None, kind=1):
+    """In place: f[k] = wr[k] + widen(narrow(f[k] - wr[k])) on non-wall nodes
+    (kind 1 = binary16, 2 = bfloat16)."""
+    assert f.dtype == np.float32 and f.flags.c_contiguous
+    Q, N = f.shape
+    wr = np.ascontiguousarray(wr, np.float32)
+    lib().lbo_quantize_dev(_p(f), Q, ctypes.c_long(N), _p(wr),
+                           _p(None if flags is None else np.ascontiguousarray(flags, np.uint8)),
+                           kind)
+
+
 def f16_roundtrip(a):
     a = np.ascontiguousarray(a, np.float32).copy()
     lib().lbo_round_storage(_p(a), ctypes.c_long(a.size), 1)

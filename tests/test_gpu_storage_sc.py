@@ -1,0 +1,177 @@
+"""GPU parity of the 16-bit deviation storage and of the D3Q19 Shan-Chen step.
+
+* FP16 / BF16 storage without Shan-Chen is bit-exact against the oracle with
+  the storage emulated (each value kept as w_k*rho_ref + widen(narrow(f -
+  w_k*rho_ref)), computed in float exactly like the kernel's load/store).
+* Shan-Chen uses psi = 1 - exp(-rho); CUDA's expf and libm may differ by an
+  ulp, so those cases carry tolerances, stated per test.
+* The spinodal error study reports rho L2 error and mass drift of the FP32,
+  FP16 and BF16 storage forms against the FP64 oracle (printed; bounds
+  asserted).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import load_package
+from golden_io import bits
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    p = load_package()
+    n = ctypes.c_int(0)
+    assert p.lib().lb_device_count(ctypes.byref(n)) == 0 and n.value >= 1, "no CUDA device"
+    return p
+
+
+def beq(a, b):
+    return np.array_equal(bits(a), bits(b))
+
+
+def channel(W, H, D):
+    fl = np.zeros((D, H, W), np.uint8)
+    fl[:, 0, :] = fl[:, -1, :] = 1
+    fl[0, :, :] = 1
+    fl[-1, :, :] = 3  # moving lid
+    z, y, x = np.mgrid[0:D, 0:H, 0:W]
+    fl[(x - W // 3) ** 2 + (y - H // 2) ** 2 + (z - D // 2) ** 2 <= 16] = 1
+    return fl.reshape(-1)
+
+
+@pytest.mark.parametrize("storage,kind", [(1, 1), (2, 2)], ids=["f16", "bf16"])
+def test_deviation_storage_bitexact(pkg, oracle, storage, kind):
+    W, H, D = 64, 20, 16
+    N = W * H * D
+    flags = channel(W, H, D)
+    rng = np.random.default_rng(30 + kind)
+    rho = (0.9 + 0.02 * rng.standard_normal(N)).astype(np.float32)
+    ux = (0.03 * rng.standard_normal(N)).astype(np.float32)
+    z = np.zeros(N, np.float32)
+    tau_inv = np.float32(1 / 0.6)
+    F = (np.float32(1e-5), np.float32(0), np.float32(0))
+    rho_ref = 0.9
+    lat = pkg.Lattice(19, W, H, D, tau_inv=tau_inv, force=F, wall_u=(0.03, 0, 0),
+                      storage=storage, rho_ref=rho_ref, graph_steps=6)
+    lat.set_flags(flags)
+    f0 = oracle.d3q19_equilibrium(rho, ux, z, z, *pkg.W3)
+    lat.set_populations(f0)
+    wr = oracle.storage_offsets(19, rho_ref)
+    f = f0.copy()
+    oracle.quantize_dev(f, wr, flags, kind)
+    fluid = (flags & 1) == 0
+    assert beq(lat.populations()[:, fluid], f[:, fluid])   # set/get round trip
+    lat.step(25)
+    corr = oracle.wall_correction(19, (0.03, 0, 0))
+    mom = [np.zeros(N, np.float32) for _ in range(4)]
+    for _ in range(25):
+        oracle.d3q19_stream_native(f, flags, corr, W, H, D)
+        oracle.d3q19_collide_native(f, flags, mom, W, H, D, *pkg.W3, tau_inv, F)
+        oracle.quantize_dev(f, wr, flags, kind)
+    assert beq(lat.populations()[:, fluid], f[:, fluid])
+    rho_g, ux_g, uy_g, uz_g = lat.moments()
+    assert beq(rho_g, mom[3]) and beq(ux_g, mom[0])
+    lat.close()
+
+
+def test_deviation_storage_equilibrium_init(pkg, oracle):
+    """lb_init_equilibrium writes the quantised equilibrium directly."""
+    W, H, D = 32, 8, 8
+    N = W * H * D
+    rng = np.random.default_rng(5)
+    rho = (0.693 * (1 + 0.01 * rng.uniform(-1, 1, N))).astype(np.float32)
+    z = np.zeros(N, np.float32)
+    lat = pkg.Lattice(19, W, H, D, storage=1, rho_ref=0.693)
+    lat.set_flags(np.zeros(N, np.uint8))
+    lat.init_equilibrium(rho, z, z, z)
+    f = oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3)
+    oracle.quantize_dev(f, oracle.storage_offsets(19, 0.693), None, 1)
+    assert beq(lat.populations(), f)
+    lat.close()
+
+
+def _spinodal_init(n, seed=2024):
+    rng = np.random.default_rng(seed)
+    eps = rng.uniform(-0.01, 0.01, n ** 3)
+    return (0.693 * (1 + eps)).astype(np.float32)
+
+
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_shan_chen_d3q19_vs_oracle(pkg, oracle, storage):
+    """D3Q19 Shan-Chen (psi = 1-exp(-rho), G = -5, tau = 1), periodic 32^3,
+    40 steps, against the float oracle with the same storage emulation: the
+    only source of difference is CUDA's expf vs libm's.  Tolerance on rho and
+    u: 2e-6 (FP32); 2e-5 with FP16 storage, where a one-ulp difference can
+    flip the rounding of a stored binary16 deviation."""
+    n = 32
+    N = n ** 3
+    rho = _spinodal_init(n, 7)
+    z = np.zeros(N, np.float32)
+    flags = np.zeros(N, np.uint8)
+    lat = pkg.Lattice(19, n, n, n, tau_inv=1.0, G=-5.0, psi_form=pkg.abi.LB_PSI_EXP1,
+                      storage=storage, rho_ref=0.693)
+    lat.set_flags(flags)
+    lat.init_equilibrium(rho, z, z, z)
+    f = oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3)
+    wr = oracle.storage_offsets(19, 0.693)
+    if storage:
+        oracle.quantize_dev(f, wr, None, storage)
+    lat.step(40)
+    mom = [np.zeros(N, np.float32) for _ in range(4)]
+    psi = np.zeros(N, np.float32)
+    zc = np.zeros(19, np.float32)
+    for _ in range(40):
+        oracle.d3q19_stream_native(f, flags, zc, n, n, n)
+        oracle.d3q19_collide_native(f, flags, mom, n, n, n, *pkg.W3, np.float32(1.0), G=-5.0,
+                                    psi=psi, psi_form=oracle.PSI_EXP1)
+        if storage:
+            oracle.quantize_dev(f, wr, None, storage)
+    rho_g, ux_g, uy_g, uz_g = lat.moments()
+    tol = 2e-6 if storage == 0 else 2e-5
+    assert np.max(np.abs(rho_g - mom[3])) <= tol
+    for a, b in zip((ux_g, uy_g, uz_g), mom[:3]):
+        assert np.max(np.abs(a - b)) <= tol
+    lat.close()
+
+
+def test_spinodal_error_vs_fp64(pkg, oracle):
+    """Error statement for the spinodal configuration at 48^3 over 300 steps:
+    rho L2 error and mass drift of FP32 / FP16 / BF16 storage (deviation from
+    w_k * 0.693) against the FP64 oracle.  Bounds: FP32 rel-L2 < 1e-5,
+    FP16 < 2e-3, BF16 < 2e-2; mass drift < 1e-4 (FP32), 1e-3 (16-bit)."""
+    n, steps = 48, 300
+    N = n ** 3
+    rho0 = _spinodal_init(n, 11)
+    z32 = np.zeros(N, np.float32)
+    flags = np.zeros(N, np.uint8)
+    f64 = oracle.d3q19_equilibrium(rho0.astype(np.float64), np.zeros(N), np.zeros(N),
+                                   np.zeros(N), 1 / 3, 1 / 18, 1 / 36)
+    mom64 = [np.zeros(N) for _ in range(4)]
+    psi64 = np.zeros(N)
+    zc = np.zeros(19)
+    for _ in range(steps):
+        oracle.d3q19_stream_native(f64, flags, zc, n, n, n)
+        oracle.d3q19_collide_native(f64, flags, mom64, n, n, n, 1 / 3, 1 / 18, 1 / 36, 1.0,
+                                    G=-5.0, psi=psi64, psi_form=oracle.PSI_EXP1)
+    rho64 = mom64[3]
+    m0 = float(np.sum(rho0.astype(np.float64)))
+    report = {}
+    for storage, name, bound, mbound in [(0, "f32", 1e-5, 1e-4), (1, "f16", 2e-3, 1e-3),
+                                         (2, "bf16", 2e-2, 1e-3)]:
+        lat = pkg.Lattice(19, n, n, n, tau_inv=1.0, G=-5.0, psi_form=pkg.abi.LB_PSI_EXP1,
+                          storage=storage, rho_ref=0.693)
+        lat.set_flags(flags)
+        lat.init_equilibrium(rho0, z32, z32, z32)
+        lat.step(steps)
+        rho = lat.moments()[0].astype(np.float64)
+        red = lat.reduce()
+        lat.close()
+        l2 = float(np.linalg.norm(rho - rho64) / np.linalg.norm(rho64))
+        drift = abs(red[0] - m0) / m0
+        report[name] = (l2, drift)
+        assert l2 < bound, (name, l2)
+        assert drift < mbound, (name, drift)
+    print("spinodal 48^3, %d steps: rho rel-L2 vs FP64 / mass drift: %s" % (steps, report))
