@@ -229,10 +229,34 @@ __device__ __forceinline__ void d2q9_zou_he_east(float (&g)[9], float rho_out) {
     g[6] = (float)((double)g[8] - (1. / 6.) * (double)ru + 0.5 * (double)(g[4] - g[2]));
 }
 
+// exp(x) in float, this library's own: Cody-Waite range reduction
+// x = k ln2 + r with ln2 split into a 12-bit head (k*head exact) and a tail,
+// |r| <= ln2/2, then the degree-7 Taylor polynomial of exp(r) (coefficients
+// 1/n! rounded to float) by Horner, scaled by 2^k.  Error at most 1.12 ulp
+// on [-87, 88].  Every operation rounds once (the library builds with
+// -fmad=false), so the oracle's copy of the same steps gives the same bits.
+__device__ __forceinline__ float lb_expf(float x) {
+    if (x < -103.f) return 0.f;
+    if (x > 88.7f) return __int_as_float(0x7f800000);
+    const float k = rintf(x * 0x1.715476p+0f);
+    const float r = (x - k * 0x1.62ep-1f) - k * 0x1.0bfbe8p-15f;
+    float p = 0x1.a01a02p-13f;
+    p = p * r + 0x1.6c16c2p-10f;
+    p = p * r + 0x1.111112p-7f;
+    p = p * r + 0x1.555556p-5f;
+    p = p * r + 0x1.555556p-3f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    const int ki = (int)k;
+    if (ki >= -126) return p * __int_as_float((ki + 127) << 23);
+    return (p * __int_as_float((ki + 64 + 127) << 23)) * 0x1p-64f;
+}
+
 // psi(rho) forms of the Shan-Chen pseudo-potential
 __device__ __forceinline__ float psi_ref(float rho) {  // src/collision.cu:293
     return (float)(4. * exp(-200. / (double)rho));
 }
-__device__ __forceinline__ float psi_exp1(float rho) { return 1.f - expf(-rho); }
+__device__ __forceinline__ float psi_exp1(float rho) { return 1.f - lb_expf(-rho); }
 
 }  // namespace lb

@@ -38,6 +38,32 @@ static const int D2_POS[4] = {1, 2, 5, 6};
 
 static inline int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
+static inline float bits_to_float(uint32_t u) { float v; memcpy(&v, &u, 4); return v; }
+
+/* exp in float by the GPU library's method (Cody-Waite reduction by ln 2 with
+ * a 12-bit head, degree-7 Taylor polynomial by Horner, scaling by 2^k): the
+ * same operations in the same order, one rounding each, so that psi =
+ * 1 - exp(-rho) is bit-identical on both sides.  Accuracy is checked against
+ * libm by tests/test_oracle_storage.py. */
+float lbo_expf(float x)
+{
+    if (x < -103.f) return 0.f;
+    if (x > 88.7f) return bits_to_float(0x7f800000u);
+    const float k = rintf(x * 0x1.715476p+0f);
+    const float r = (x - k * 0x1.62ep-1f) - k * 0x1.0bfbe8p-15f;
+    float p = 0x1.a01a02p-13f;
+    p = p * r + 0x1.6c16c2p-10f;
+    p = p * r + 0x1.111112p-7f;
+    p = p * r + 0x1.555556p-5f;
+    p = p * r + 0x1.555556p-3f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    const int ki = (int)k;
+    if (ki >= -126) return p * bits_to_float((uint32_t)(ki + 127) << 23);
+    return (p * bits_to_float((uint32_t)(ki + 64 + 127) << 23)) * 0x1p-64f;
+}
+
 #define R float
 #define S f32
 #include "lb_oracle_body.h"

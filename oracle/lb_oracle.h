@@ -93,6 +93,9 @@ void lbo_round_storage(float *f, long n, int kind /* 1 = f16, 2 = bf16 */);
  * f[k][o] = wr[k] + widen(narrow_rne(f[k][o] - wr[k])), all in float */
 void lbo_quantize_dev(float *f, int Q, long N, const float *wr, const uint8_t *flags, int kind);
 
+/* exp in float by the GPU library's own method (same operations) */
+float lbo_expf(float x);
+
 int lbo_num_threads(void);
 void lbo_set_threads(int n);
 

@@ -211,7 +211,7 @@ static inline void FN(d2q9_moments)(const R *g, R *rho, R *ux, R *uy)
 static inline R FN(psi_of)(R rho, int form)
 {
     if (form == LBO_PSI_REF) return (R)(4. * exp(-200. / (double)rho));
-    return (R)1 - (sizeof(R) == sizeof(float) ? (R)expf((float)-rho) : (R)exp((double)-rho));
+    return (R)1 - (sizeof(R) == sizeof(float) ? (R)lbo_expf((float)-rho) : (R)exp((double)-rho));
 }
 
 /* Shan-Chen interaction + adhesion force and BGK, the second launch of the

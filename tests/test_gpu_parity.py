@@ -314,10 +314,9 @@ def test_context_reference_d2q9_shan_chen_vs_oracle(pkg, oracle):
     lat.close()
 
 
-def test_context_native_d2q9_shan_chen_tolerance(pkg, oracle):
-    """psi = 1-exp(-rho): CUDA's expf and libm may differ by an ulp, so this
-    case is compared with a tolerance: |drho| <= 1e-5 and |du| <= 1e-6 after
-    50 steps (FP32 noise level of rho ~ 1)."""
+def test_context_native_d2q9_shan_chen(pkg, oracle):
+    """Native D2Q9 Shan-Chen with psi = 1-exp(-rho) (exp evaluated by the
+    library's own float function on both sides), 50 steps, bit-exact."""
     W, H = 64, 64
     N = W * H
     rng = np.random.default_rng(10)
@@ -335,9 +334,8 @@ def test_context_native_d2q9_shan_chen_tolerance(pkg, oracle):
         oracle.d2q9_collide_native(f, np.zeros(N, np.uint8), mom, W, H, *pkg.W2, 1.0, G=-5.0,
                                    psi_form=oracle.PSI_EXP1)
     rho_g, ux_g, uy_g, _ = lat.moments()
-    assert np.max(np.abs(rho_g - mom[2])) <= 1e-5
-    assert np.max(np.abs(ux_g - mom[0])) <= 1e-6
-    assert np.max(np.abs(uy_g - mom[1])) <= 1e-6
+    assert beq(rho_g, mom[2]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1])
+    assert beq(lat.populations(), f)
     lat.close()
 
 

@@ -102,10 +102,9 @@ def _spinodal_init(n, seed=2024):
 @pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
 def test_shan_chen_d3q19_vs_oracle(pkg, oracle, storage):
     """D3Q19 Shan-Chen (psi = 1-exp(-rho), G = -5, tau = 1), periodic 32^3,
-    40 steps, against the float oracle with the same storage emulation: the
-    only source of difference is CUDA's expf vs libm's.  Tolerance on rho and
-    u: 2e-6 (FP32); 2e-5 with FP16 storage, where a one-ulp difference can
-    flip the rounding of a stored binary16 deviation."""
+    40 steps, bit-exact against the float oracle with the same storage
+    emulation (both sides evaluate exp with the library's own float
+    function, so nothing differs)."""
     n = 32
     N = n ** 3
     rho = _spinodal_init(n, 7)
@@ -130,10 +129,10 @@ def test_shan_chen_d3q19_vs_oracle(pkg, oracle, storage):
         if storage:
             oracle.quantize_dev(f, wr, None, storage)
     rho_g, ux_g, uy_g, uz_g = lat.moments()
-    tol = 2e-6 if storage == 0 else 2e-5
-    assert np.max(np.abs(rho_g - mom[3])) <= tol
+    assert beq(rho_g, mom[3])
     for a, b in zip((ux_g, uy_g, uz_g), mom[:3]):
-        assert np.max(np.abs(a - b)) <= tol
+        assert beq(a, b)
+    assert beq(lat.populations(), f)
     lat.close()
 
 

@@ -36,6 +36,22 @@ def test_bf16_roundtrip_matches_integer_reference(oracle):
     assert np.array_equal(got.view(np.uint32), exp.view(np.uint32))
 
 
+def test_expf_accuracy(oracle):
+    """The float exp shared by the kernels and the oracle (Cody-Waite + Taylor)
+    stays within 1.5 ulp of exp on [-20, 0] and [-87, 88] (1.12 measured)."""
+    import ctypes
+    fn = oracle.lib().lbo_expf
+    fn.restype = ctypes.c_float
+    fn.argtypes = [ctypes.c_float]
+    for lo, hi, tol in [(-20.0, 0.0, 1.5), (-87.0, 88.0, 1.5)]:
+        xs = np.linspace(lo, hi, 20001).astype(np.float32)
+        got = np.array([fn(float(x)) for x in xs], np.float64)
+        exact = np.exp(xs.astype(np.float64))
+        ulp = np.spacing(exact.astype(np.float32)).astype(np.float64)
+        assert np.max(np.abs(got - exact) / ulp) <= tol
+    assert fn(-200.0) == 0.0 and fn(100.0) == float("inf")
+
+
 def test_quantize_dev_keeps_walls(oracle):
     rng = np.random.default_rng(3)
     f = rng.random((19, 1000)).astype(np.float32)
