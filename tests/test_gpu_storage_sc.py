@@ -144,8 +144,8 @@ def test_spinodal_error_vs_fp64(pkg, oracle):
     the 300-step figures measure that growth, not a per-step error.  err =
     |rho - rho64|_2 / |rho64 - mean|_2 (relative to the density fluctuation).
     Bounds (loose; the printed figures are the statement): at 50 steps FP32
-    1e-3, 16-bit 0.2; at 300 steps 1.0; mass drift 5e-5 (FP32), 1e-3
-    (16-bit)."""
+    1e-3, 16-bit 0.2; at 300 steps 1.0; mass drift 5e-5 (FP32), 1e-3 (FP16),
+    1e-2 (BF16)."""
     n, horizons = 48, (50, 300)
     N = n ** 3
     rho0 = _spinodal_init(n, 11)
@@ -188,4 +188,4 @@ def test_spinodal_error_vs_fp64(pkg, oracle):
     for key, v in report.items():
         name, h = key.split("@")
         assert v["err"] < ({"f32": 1e-3}.get(name, 0.2) if h == "50" else 1.0), (key, v)
-        assert v["mass_drift"] < (5e-5 if name == "f32" else 1e-3), (key, v)
+        assert v["mass_drift"] < {"f32": 5e-5, "f16": 1e-3, "bf16": 1e-2}[name], (key, v)
