@@ -351,13 +351,13 @@ def main():
 
 
 def measure_e2e(pkg, L, wl, flags, steps, ws, dist):
-    """The reference's per-step host sequence (streaming_d3q19,
-    collision_d3q19 with moments and plot, read_value_3d, 16-byte probe copy)
-    through the drop-in entry points in fused mode, driven by the library's
-    native host loop lb_run_lbm_d3q19; the initial populations and walls are
-    uploaded from pinned host memory and the final moment fields read back
-    inside the timed region.  Reference semantics (Zou-He x faces, walls
-    stored full-way) on the same lattice and walls."""
+    """End to end through the library's C ABI with host buffers: the initial
+    populations are uploaded from pinned host memory (lb_set_populations),
+    then lb_run_probe runs the reference's per-step host pattern (one step
+    that writes the moment fields, then a read_value-style probe of one node
+    copied to the host and waited for, every step), and the final rho and u
+    fields are read back into pinned host memory -- all inside the timed
+    region.  Same workload and physics as the device-resident number."""
     import ctypes as C
     N = wl.N
     nx, ny, nz = wl.size
@@ -372,51 +372,44 @@ def measure_e2e(pkg, L, wl, flags, steps, ws, dist):
         buf = (C.c_uint8 * n).from_address(p.value)
         return np.frombuffer(buf, dtype=dtype).reshape(shape)
 
-    w = pkg.W3
-    # inputs in pinned memory: equilibrium populations at rho = 1, u = 0 (= w_k) and walls
-    f_host = pinned((19, N), np.float32)
-    for k in range(19):
-        f_host[k] = w[0] if k == 0 else (w[1] if k <= 6 else w[2])
-    solid = pinned((N,), np.uint8)
-    solid[:] = flags & 1
-    sb = pinned((N,), np.uint8)
-    sb[:] = 0
+    w = pkg.W3 if wl.lattice == 19 else pkg.W2
+    Q = wl.lattice
+    f_host = pinned((Q, N), np.float32)
+    for k in range(Q):  # equilibrium at rho = 1, u = 0 is w_k
+        f_host[k] = w[0] if k == 0 else (w[1] if k <= (6 if Q == 19 else 4) else w[2])
     out_fields = [pinned((N,), np.float32) for _ in range(4)]
-    dd = pkg.DeviceData(19, nx, ny, nz)
-    assert L.lb_abi_set_mode(pkg.abi.LB_ABI_FUSED) == 0
-    params = pkg.abi.lb_run_params_d3q19(w[0], w[1], w[2], np.float32(1 / wl.tau), 0.0, 0.0,
-                                         0.0, 1.0, (C.c_int * 3)(nx // 2, ny // 2, nz // 2))
-    value = np.zeros(4, np.float32)
-    # warm-up (allocates the library's second population set)
-    dd.upload(f_host)
-    dd.set_solid(solid, sb)
-    assert L.lb_run_lbm_d3q19(dd.ptr(), C.c_void_p(dd.plot), C.byref(params), 3,
-                              value.ctypes.data_as(C.c_void_p)) == 0
-    L.lb_device_synchronize()
+    value = pinned((4,), np.float32)
+    lat = pkg.Lattice(wl.lattice, nx, ny, nz, tau_inv=np.float32(1 / wl.tau),
+                      force=tuple(np.float32(v) for v in wl.force), wall_u=wl.wall_u)
+    lat.set_flags(flags)
+    cx, cy, cz = nx // 2, ny // 3, nz // 2
+    vp = value.ctypes.data_as(C.c_void_p)
+    # warm-up
+    assert L.lb_set_populations(lat.h, f_host.ctypes.data_as(C.c_void_p)) == 0
+    assert L.lb_run_probe(lat.h, 3, cx, cy, cz, vp) == 0
+    lat.synchronize()
     if dist:
         dist.barrier()
+    n0 = lat.launches()
     t0 = time.perf_counter()
-    dd.upload(f_host)
-    dd.set_solid(solid, sb)
-    rc = L.lb_run_lbm_d3q19(dd.ptr(), C.c_void_p(dd.plot), C.byref(params), steps,
-                            value.ctypes.data_as(C.c_void_p))
-    for name, dst in zip(("rho", "ux", "uy", "uz"), out_fields):
-        L.lb_memcpy_d2h(dst.ctypes.data_as(C.c_void_p), C.c_void_p(getattr(dd.s, name)), 4 * N)
-    L.lb_device_synchronize()
+    rc1 = L.lb_set_populations(lat.h, f_host.ctypes.data_as(C.c_void_p))
+    rc2 = L.lb_run_probe(lat.h, steps, cx, cy, cz, vp)
+    rc3 = L.lb_get_moments(lat.h, *[a.ctypes.data_as(C.c_void_p) for a in out_fields])
     el = time.perf_counter() - t0
-    assert rc == 0, L.lb_abi_last_error()
+    assert rc1 == rc2 == rc3 == 0, L.lb_error(lat.h)
+    launches = lat.launches() - n0
     el = dist_max(dist, el)
-    L.lb_abi_set_mode(pkg.abi.LB_ABI_STANDALONE)
-    assert np.isfinite(out_fields[0]).all()
-    dd.close()
+    assert np.isfinite(out_fields[0]).all() and np.isfinite(value).all()
+    lat.close()
     for p in pinned_ptrs:
         L.lb_free_host(p)
-    h2d = 19 * 4 * N + 2 * N
+    h2d = 4 * Q * N
     d2h = 16 * steps + 4 * 4 * N
     return {"value": ws * N * steps / el / 1e9, "unit": "GLUPS",
             "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
-            "steps": steps, "path": "reference entry points (fused mode) via lb_run_lbm_d3q19",
-            "physics": "reference semantics on the same lattice and walls"}
+            "steps": steps, "gpu_launches": launches,
+            "path": "lb_set_populations + lb_run_probe (step with moments, 16-byte probe copy "
+                    "each step) + lb_get_moments, pinned host buffers, wall clock"}
 
 
 if __name__ == "__main__":

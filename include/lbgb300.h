@@ -206,6 +206,13 @@ int lb_step(lb_ctx *ctx, int nsteps);
 int lb_get_moments(lb_ctx *ctx, float *rho, float *ux, float *uy, float *uz);
 /* conservation sums of the last step's moments, FP64 (see lb_reduce_d3q19) */
 int lb_reduce(lb_ctx *ctx, double out[7]);
+/* (ux, uy, uz, rho) of the last step at one node, copied to host memory
+ * (blocks until the copy is done) -- the context form of read_value_3d */
+int lb_probe(lb_ctx *ctx, int x, int y, int z, float value[4]);
+/* the reference's per-step host pattern on a context: nsteps times one step
+ * that writes the moment fields, then lb_probe at (x, y, z); value[4] holds
+ * the last probe */
+int lb_run_probe(lb_ctx *ctx, int nsteps, int x, int y, int z, float value[4]);
 int lb_synchronize(lb_ctx *ctx);
 /* run nsteps and return the device time between CUDA events recorded on the
  * context's stream (warm-up is the caller's business) */

@@ -125,6 +125,9 @@ PROTOTYPES = [
     ("lb_get_moments", _c.c_int, [_c.c_void_p] * 5),
     ("lb_reduce", _c.c_int, [_c.c_void_p, _c.POINTER(_c.c_double)]),
     ("lb_synchronize", _c.c_int, [_c.c_void_p]),
+    ("lb_probe", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_int, _c.c_int, _c.c_void_p]),
+    ("lb_run_probe", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
+                                _c.c_void_p]),
     ("lb_time_steps", _c.c_int, [_c.c_void_p, _c.c_int, _c.POINTER(_c.c_float)]),
     ("lb_launch_count", _c.c_int64, [_c.c_void_p]),
     ("lb_wall_correction", _c.c_int, [_c.c_void_p, _c.c_void_p]),

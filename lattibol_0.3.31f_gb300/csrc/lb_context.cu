@@ -265,7 +265,8 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sb, c->stride);
     if (e == cudaSuccess) e = cudaMalloc(&c->mom, sizeof(float) * c->stride * 4);
     if (e == cudaSuccess && nsc) e = cudaMalloc(&c->sc, sizeof(float) * c->stride * nsc);
-    if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 8));
+    // reduction partials, 7 results, then 4 floats (2 doubles) for lb_probe
+    if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 16));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -436,6 +437,34 @@ int lb_reduce(lb_ctx *c, double out[7]) {
     c->launches += 2;
     LB_TRY(c, "lb_reduce", cudaMemcpyAsync(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
     LB_TRY(c, "lb_reduce", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_probe(lb_ctx *c, int x, int y, int z, float value[4]) {
+    if (!c || !value) return LB_ERR_ARG;
+    if (x < 0 || y < 0 || z < 0 || x >= c->cfg.nx || y >= c->cfg.ny || z >= c->cfg.nz)
+        return fail(c, LB_ERR_ARG, "lb_probe: node outside the lattice");
+    const long o = x + (long)c->cfg.nx * (y + (long)c->cfg.ny * z);
+    // the 4 floats land in the reduction scratch, after partials and results
+    float *dev = reinterpret_cast<float *>(c->red + reduce_partials_size() + 7);
+    LB_TRY(c, "lb_probe",
+           launch_read_value(nullptr, mom_k(c, 1), mom_k(c, 2), c->Q == 19 ? mom_k(c, 3) : nullptr,
+                             mom_k(c, 0), dev, o, c->stream));
+    c->launches += 1;
+    LB_TRY(c, "lb_probe", cudaMemcpyAsync(value, dev, 4 * sizeof(float), cudaMemcpyDeviceToHost,
+                                          c->stream));
+    LB_TRY(c, "lb_probe", cudaStreamSynchronize(c->stream));
+    return LB_OK;
+}
+
+int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
+    if (!c || !value || nsteps < 0) return LB_ERR_ARG;
+    for (int i = 0; i < nsteps; i++) {
+        LB_TRY(c, "lb_run_probe", step_once(c, c->cur, true));
+        c->cur = 1 - c->cur;
+        const int rc = lb_probe(c, x, y, z, value);
+        if (rc != LB_OK) return rc;
+    }
     return LB_OK;
 }
 
