@@ -223,6 +223,39 @@ int64_t lb_launch_count(const lb_ctx *ctx);
  * by the kernels (q = 9 or 19 floats) */
 int lb_wall_correction(const lb_ctx *ctx, float *corr);
 
+/* ======================================================================== */
+/* Part 3: ensembles of independent periodic D2Q9 Shan-Chen domains        */
+/* ======================================================================== */
+/* Many small lattices of different sizes advanced together: one packed
+ * population slab (domain d at nodes [offset(d), offset(d) + nx[d]*ny[d]),
+ * node x + nx[d]*y inside it), two persistent launches per step over a work
+ * list of row groups, batches replayed from a captured CUDA graph.  Each
+ * domain is periodic, without walls or body force, with its own G and
+ * tau_inv; a domain evolves bit for bit like the same lattice run alone
+ * through the context API (native mode, same psi form). */
+typedef struct lb_ensemble lb_ensemble;
+int lb_ensemble_create(int ndomains, const int *nx, const int *ny, const float *G,
+                       const float *tau_inv, int psi_form, lb_ensemble **out);
+int lb_ensemble_destroy(lb_ensemble *e);
+const char *lb_ensemble_error(const lb_ensemble *e);
+long lb_ensemble_nodes(const lb_ensemble *e);          /* total nodes of all domains */
+long lb_ensemble_offset(const lb_ensemble *e, int d);  /* first node of domain d */
+/* populations f[k*nodes + node] / equilibrium at u = 0 from a packed density */
+int lb_ensemble_set_populations(lb_ensemble *e, const float *f);
+int lb_ensemble_get_populations(lb_ensemble *e, float *f);
+int lb_ensemble_init_equilibrium(lb_ensemble *e, const float *rho);
+int lb_ensemble_step(lb_ensemble *e, int nsteps);  /* last step writes the moments */
+int lb_ensemble_time_steps(lb_ensemble *e, int nsteps, float *ms);
+int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy);
+/* launch shape: threads along x (multiple of 32), rows per work item, blocks
+ * per SM; the autotuner times every candidate for trial_steps steps on the
+ * ensemble itself (advancing its state: tune before initialising) and keeps
+ * the fastest, returned in out[3] */
+int lb_ensemble_set_launch(lb_ensemble *e, int threads_x, int rows, int blocks_per_sm);
+int lb_ensemble_get_launch(const lb_ensemble *e, int out[3]);
+int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]);
+int64_t lb_ensemble_launch_count(const lb_ensemble *e);
+
 /* ---- device helpers (tests and hosts without their own allocator) ------ */
 int lb_device_count(int *n);
 int lb_malloc(void **ptr, size_t bytes);

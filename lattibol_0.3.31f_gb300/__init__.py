@@ -17,4 +17,5 @@ def lib():
     return _lib
 
 
-from .lattice import DeviceData, Lattice, LBError, W2, W3  # noqa: E402,F401
+from .lattice import (DeviceData, Ensemble, Lattice, LBError, W2, W3,  # noqa: E402,F401
+                      droplet_ensemble)

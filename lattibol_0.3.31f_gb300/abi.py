@@ -131,6 +131,22 @@ PROTOTYPES = [
     ("lb_time_steps", _c.c_int, [_c.c_void_p, _c.c_int, _c.POINTER(_c.c_float)]),
     ("lb_launch_count", _c.c_int64, [_c.c_void_p]),
     ("lb_wall_correction", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_ensemble_create", _c.c_int, [_c.c_int, _c.c_void_p, _c.c_void_p, _c.c_void_p,
+                                      _c.c_void_p, _c.c_int, _c.POINTER(_c.c_void_p)]),
+    ("lb_ensemble_destroy", _c.c_int, [_c.c_void_p]),
+    ("lb_ensemble_error", _c.c_char_p, [_c.c_void_p]),
+    ("lb_ensemble_nodes", _c.c_long, [_c.c_void_p]),
+    ("lb_ensemble_offset", _c.c_long, [_c.c_void_p, _c.c_int]),
+    ("lb_ensemble_set_populations", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_ensemble_get_populations", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_ensemble_init_equilibrium", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_ensemble_step", _c.c_int, [_c.c_void_p, _c.c_int]),
+    ("lb_ensemble_time_steps", _c.c_int, [_c.c_void_p, _c.c_int, _c.POINTER(_c.c_float)]),
+    ("lb_ensemble_get_moments", _c.c_int, [_c.c_void_p] * 4),
+    ("lb_ensemble_set_launch", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_int, _c.c_int]),
+    ("lb_ensemble_get_launch", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_ensemble_autotune", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p]),
+    ("lb_ensemble_launch_count", _c.c_int64, [_c.c_void_p]),
     ("lb_device_count", _c.c_int, [_c.POINTER(_c.c_int)]),
     ("lb_malloc", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
     ("lb_free", _c.c_int, [_c.c_void_p]),

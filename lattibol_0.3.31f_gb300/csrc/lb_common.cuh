@@ -229,6 +229,32 @@ __device__ __forceinline__ void d2q9_zou_he_east(float (&g)[9], float rho_out) {
     g[6] = (float)((double)g[8] - (1. / 6.) * (double)ru + 0.5 * (double)(g[4] - g[2]));
 }
 
+// Shan-Chen interaction of the D2Q9 step, reference src/collision.cu:78-96:
+// F = -G psi(x) sum_k w_k psi(x + c_k) c_k accumulated in the reference's
+// order, then u_eq += F / (tau_inv rho).  ps[m] is psi at the reference's
+// stencil slot m (0 centre, 1 x+1, 2 row+1, 3 x-1, 4 row-1, 5 (x+1,row+1),
+// 6 (x-1,row+1), 7 (x-1,row-1), 8 (x+1,row-1)).
+__device__ __forceinline__ void d2q9_sc_shift(const float (&ps)[9], float w1, float w5, float G,
+                                              float tau_inv, float rho, float &ex, float &ey) {
+    float IFx = 0.f, IFy = 0.f;
+    IFx = IFx + w1 * ps[1];
+    IFx = IFx - w1 * ps[3];
+    IFx = IFx + w5 * ps[5];
+    IFx = IFx - w5 * ps[6];
+    IFx = IFx - w5 * ps[7];
+    IFx = IFx + w5 * ps[8];
+    IFy = IFy - w1 * ps[2];
+    IFy = IFy + w1 * ps[4];
+    IFy = IFy - w5 * ps[5];
+    IFy = IFy - w5 * ps[6];
+    IFy = IFy + w5 * ps[7];
+    IFy = IFy + w5 * ps[8];
+    IFx = -G * ps[0] * IFx;
+    IFy = -G * ps[0] * IFy;
+    ex = ex + (IFx / (tau_inv * rho));
+    ey = ey + (IFy / (tau_inv * rho));
+}
+
 // exp(x) in float, this library's own: Cody-Waite range reduction
 // x = k ln2 + r with ln2 split into a 12-bit head (k*head exact) and a tail,
 // |r| <= ln2/2, then the degree-7 Taylor polynomial of exp(r) (coefficients

@@ -122,24 +122,12 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_sc_kernel(const D2Args a) {
     const int m5 = yp * W + xp, m6 = yp * W + xn, m7 = yn * W + xn, m8 = yn * W + xp;
     const float *psi = a.psi;
     const float w1 = a.w1, w5 = a.w5;
-    float IFx = 0.f, IFy = 0.f;
-    IFx = IFx + w1 * __ldg(psi + m1);
-    IFx = IFx - w1 * __ldg(psi + m3);
-    IFx = IFx + w5 * __ldg(psi + m5);
-    IFx = IFx - w5 * __ldg(psi + m6);
-    IFx = IFx - w5 * __ldg(psi + m7);
-    IFx = IFx + w5 * __ldg(psi + m8);
-    IFy = IFy - w1 * __ldg(psi + m2);
-    IFy = IFy + w1 * __ldg(psi + m4);
-    IFy = IFy - w5 * __ldg(psi + m5);
-    IFy = IFy - w5 * __ldg(psi + m6);
-    IFy = IFy + w5 * __ldg(psi + m7);
-    IFy = IFy + w5 * __ldg(psi + m8);
-    const float p0 = psi[o], rho = a.rho[o];
-    IFx = -a.G * p0 * IFx;
-    IFy = -a.G * p0 * IFy;
-    float ex = a.ueq_x[o] + (IFx / (a.tau_inv * rho));
-    float ey = a.ueq_y[o] + (IFy / (a.tau_inv * rho));
+    const float ps[9] = {psi[o],           __ldg(psi + m1), __ldg(psi + m2),
+                         __ldg(psi + m3),  __ldg(psi + m4), __ldg(psi + m5),
+                         __ldg(psi + m6),  __ldg(psi + m7), __ldg(psi + m8)};
+    const float p0 = ps[0], rho = a.rho[o];
+    float ex = a.ueq_x[o], ey = a.ueq_y[o];
+    d2q9_sc_shift(ps, w1, w5, a.G, a.tau_inv, rho, ex, ey);
     if (a.Gads != 0.f) {
         const uint8_t *s = a.flags;
         float Fsx = 0.f, Fsy = 0.f;

@@ -127,6 +127,108 @@ class Lattice:
         return c
 
 
+def droplet_ensemble(ndomains, seed=4, side_choices=None, width=2.0):
+    """Seeded droplet ensemble: side lengths uniform over the multiples of 32
+    in [64, 512], G ~ U[-5.5, -4.5], one centred droplet of radius
+    U[0.1, 0.3]*side at rho_liquid = 2.0 in vapour at rho = 0.1 (interface
+    smoothed by tanh over `width` nodes).  Returns (nx, ny, G, packed rho)."""
+    rng = np.random.default_rng(seed)
+    sides = np.asarray(side_choices if side_choices is not None else np.arange(64, 513, 32))
+    nx = rng.choice(sides, ndomains).astype(np.int32)
+    ny = nx.copy()
+    G = rng.uniform(-5.5, -4.5, ndomains).astype(np.float32)
+    frac = rng.uniform(0.1, 0.3, ndomains)
+    rhos = []
+    for d in range(ndomains):
+        n = int(nx[d])
+        y, x = np.mgrid[0:n, 0:n]
+        r = np.sqrt((x - (n - 1) / 2.0) ** 2 + (y - (n - 1) / 2.0) ** 2)
+        R = frac[d] * n
+        rho = 1.05 - 0.95 * np.tanh((r - R) / width)
+        rhos.append(rho.astype(np.float32).reshape(-1))
+    return nx, ny, G, np.concatenate(rhos)
+
+
+class Ensemble:
+    """Independent periodic D2Q9 Shan-Chen domains advanced together
+    (lb_ensemble_* of the C ABI)."""
+
+    def __init__(self, nx, ny, G, tau_inv=None, psi_form=abi.LB_PSI_EXP1):
+        L = _lib()
+        self.nx = np.ascontiguousarray(nx, np.int32)
+        self.ny = np.ascontiguousarray(ny, np.int32)
+        self.G = np.ascontiguousarray(G, np.float32)
+        nd = len(self.nx)
+        self.tau_inv = np.ascontiguousarray(np.ones(nd) if tau_inv is None else tau_inv,
+                                            np.float32)
+        h = ctypes.c_void_p()
+        rc = L.lb_ensemble_create(nd, _ptr(self.nx), _ptr(self.ny), _ptr(self.G),
+                                  _ptr(self.tau_inv), psi_form, ctypes.byref(h))
+        if rc != abi.LB_OK:
+            raise LBError("lb_ensemble_create failed: %d" % rc)
+        self.h = h
+        self.NT = L.lb_ensemble_nodes(h)
+        self.offsets = [L.lb_ensemble_offset(h, d) for d in range(nd)]
+
+    def _check(self, rc, what):
+        if rc != abi.LB_OK:
+            raise LBError("%s: %d %s" % (what, rc, _lib().lb_ensemble_error(self.h).decode()))
+
+    def close(self):
+        if self.h:
+            _lib().lb_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_equilibrium(self, rho):
+        rho = np.ascontiguousarray(rho, np.float32)
+        self._check(_lib().lb_ensemble_init_equilibrium(self.h, _ptr(rho)), "init")
+
+    def set_populations(self, f):
+        f = np.ascontiguousarray(f, np.float32)
+        self._check(_lib().lb_ensemble_set_populations(self.h, _ptr(f)), "set_populations")
+
+    def populations(self):
+        f = np.empty((9, self.NT), np.float32)
+        self._check(_lib().lb_ensemble_get_populations(self.h, _ptr(f)), "get_populations")
+        return f
+
+    def step(self, n):
+        self._check(_lib().lb_ensemble_step(self.h, int(n)), "step")
+
+    def time_steps(self, n):
+        ms = ctypes.c_float()
+        self._check(_lib().lb_ensemble_time_steps(self.h, int(n), ctypes.byref(ms)), "time")
+        return ms.value
+
+    def moments(self):
+        out = [np.empty(self.NT, np.float32) for _ in range(3)]
+        self._check(_lib().lb_ensemble_get_moments(self.h, *[_ptr(a) for a in out]), "moments")
+        return tuple(out)
+
+    def set_launch(self, threads_x, rows, blocks_per_sm):
+        self._check(_lib().lb_ensemble_set_launch(self.h, threads_x, rows, blocks_per_sm),
+                    "set_launch")
+
+    def autotune(self, trial_steps=3):
+        out = np.zeros(3, np.int32)
+        self._check(_lib().lb_ensemble_autotune(self.h, trial_steps, _ptr(out)), "autotune")
+        return tuple(int(v) for v in out)
+
+    def launches(self):
+        return _lib().lb_ensemble_launch_count(self.h)
+
+    def domain(self, arr, d):
+        """The slice of a packed per-node array belonging to domain d."""
+        o = self.offsets[d]
+        return arr[..., o:o + int(self.nx[d]) * int(self.ny[d])]
+
+
 class DeviceData:
     """The reference's per-device struct with every array on the GPU.
 
