@@ -125,9 +125,12 @@ ENSEMBLE = {"domains": 512, "steps": 5000, "seed": 4,
 def run_ensemble(args, dist, ws, rank, local):
     """The batched ensemble: 512 independent periodic D2Q9 Shan-Chen droplet
     domains (sides uniform over the multiples of 32 in [64, 512], G ~
-    U[-5.5, -4.5], droplet rho_l = 2.0 of radius U[0.1, 0.3]*side in vapour
-    rho = 0.1, tau = 1), autotuned launch shape, CUDA-graph-replayed
-    persistent launches.  GLUPS counts the nodes of all domains."""
+    U[-5.5, -4.5], one droplet of radius U[0.1, 0.3]*side, tau = 1),
+    autotuned launch shape, CUDA-graph-replayed persistent launches.  Each
+    droplet starts at the coexistence densities of its own G (liquid 1.49 ..
+    2.31, vapour 0.25 .. 0.10): the fixed pair 2.0 / 0.1 is far from
+    coexistence for G near -4.5 and those droplets blow up within 300 steps.
+    GLUPS counts the nodes of all domains."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     nx, ny, G, rho = pkg.droplet_ensemble(ENSEMBLE["domains"], seed=ENSEMBLE["seed"])
@@ -156,6 +159,8 @@ def run_ensemble(args, dist, ws, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "ensemble_512_d2q9_shan_chen_droplets", "domains": len(nx),
+                       "droplet": "radius U[0.1,0.3]*side at the coexistence densities of "
+                                  "its G (tanh interface, width 2)",
                        "total_nodes": NT, "sides": "multiples of 32 in [64, 512], seed %d"
                        % ENSEMBLE["seed"], "G": "U[-5.5,-4.5]", "tau": 1.0,
                        "psi": "1-exp(-rho)", "launch_shape": {"threads_x": shape[0],

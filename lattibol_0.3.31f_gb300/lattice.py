@@ -127,11 +127,53 @@ class Lattice:
         return c
 
 
-def droplet_ensemble(ndomains, seed=4, side_choices=None, width=2.0):
+def sc_coexistence(G, n=4000):
+    """Liquid and vapour densities of the Shan-Chen fluid with psi = 1-exp(-rho)
+    (pressure p = rho/3 + G psi^2 / 6) at coexistence, from the mechanical
+    stability condition of Shan & Chen: p(rho_v) = p(rho_l) = p0 and
+    integral_{rho_v}^{rho_l} (p0 - p) psi'/psi^2 drho = 0, solved for p0 by
+    bisection between the spinodal pressures."""
+    G = float(G)
+    rho = np.linspace(1e-3, 6.0, 24001)
+    psi = 1 - np.exp(-rho)
+    p = rho / 3 + G * psi ** 2 / 6
+    dp = np.gradient(p, rho)
+    neg = np.where(dp < 0)[0]
+    if len(neg) == 0:
+        raise ValueError("G = %g is above the critical coupling (no coexistence)" % G)
+    i_max, i_min = neg[0], neg[-1]  # local maximum and minimum of p(rho)
+    p_hi, p_lo = p[i_max], p[i_min]
+
+    def roots(p0):
+        rv = np.interp(p0, p[:i_max + 1], rho[:i_max + 1])            # p rising on [0, i_max]
+        rl = np.interp(p0, p[i_min:], rho[i_min:])                     # p rising after i_min
+        return rv, rl
+
+    def excess(p0):
+        rv, rl = roots(p0)
+        r = np.linspace(rv, rl, n)
+        s = 1 - np.exp(-r)
+        integrand = (p0 - (r / 3 + G * s ** 2 / 6)) * np.exp(-r) / s ** 2
+        return float(np.sum((integrand[1:] + integrand[:-1]) * np.diff(r)) / 2)
+
+    # excess grows with p0: a positive excess means p0 is above coexistence
+    lo, hi = max(p_lo, p[0]), p_hi
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        if excess(mid) > 0:
+            hi = mid
+        else:
+            lo = mid
+    return roots(0.5 * (lo + hi))[::-1]  # (rho_liquid, rho_vapour)
+
+
+def droplet_ensemble(ndomains, seed=4, side_choices=None, width=2.0, densities="coexistence"):
     """Seeded droplet ensemble: side lengths uniform over the multiples of 32
     in [64, 512], G ~ U[-5.5, -4.5], one centred droplet of radius
-    U[0.1, 0.3]*side at rho_liquid = 2.0 in vapour at rho = 0.1 (interface
-    smoothed by tanh over `width` nodes).  Returns (nx, ny, G, packed rho)."""
+    U[0.1, 0.3]*side (interface smoothed by tanh over `width` nodes).
+    densities = (rho_liquid, rho_vapour) for every domain, or "coexistence":
+    each domain starts at the coexistence pair of its own G (sc_coexistence).
+    Returns (nx, ny, G, packed rho)."""
     rng = np.random.default_rng(seed)
     sides = np.asarray(side_choices if side_choices is not None else np.arange(64, 513, 32))
     nx = rng.choice(sides, ndomains).astype(np.int32)
@@ -141,10 +183,11 @@ def droplet_ensemble(ndomains, seed=4, side_choices=None, width=2.0):
     rhos = []
     for d in range(ndomains):
         n = int(nx[d])
+        rl, rv = sc_coexistence(G[d]) if densities == "coexistence" else densities
         y, x = np.mgrid[0:n, 0:n]
         r = np.sqrt((x - (n - 1) / 2.0) ** 2 + (y - (n - 1) / 2.0) ** 2)
         R = frac[d] * n
-        rho = 1.05 - 0.95 * np.tanh((r - R) / width)
+        rho = 0.5 * (rl + rv) - 0.5 * (rl - rv) * np.tanh((r - R) / width)
         rhos.append(rho.astype(np.float32).reshape(-1))
     return nx, ny, G, np.concatenate(rhos)
 
