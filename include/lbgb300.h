@@ -256,6 +256,48 @@ int lb_ensemble_get_launch(const lb_ensemble *e, int out[3]);
 int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]);
 int64_t lb_ensemble_launch_count(const lb_ensemble *e);
 
+/* ======================================================================== */
+/* Part 4: learned sub-grid closure (D3Q19)                                 */
+/* ======================================================================== */
+/* A 19 -> 64 -> 64 -> 1 ReLU network maps each cell's non-equilibrium
+ * moments and |S| to an eddy viscosity nu_t = nu0 * clamp(y, 0, z_max); the
+ * closure kernel relaxes the cell with tau = 0.5 + 3 (nu0 + nu_t).  The
+ * network runs on the tensor cores (BF16 weights and activations, FP32
+ * accumulate) inside the collision kernel; training uses the same forward
+ * pass, an FP32 backward pass and Adam, all on the GPU. */
+typedef struct lb_mlp lb_mlp;
+int lb_mlp_create(uint64_t seed, lb_mlp **out);  /* He-uniform initial weights */
+int lb_mlp_destroy(lb_mlp *m);
+const char *lb_mlp_error(const lb_mlp *m);
+int lb_mlp_num_params(void);  /* 5505: W1[64][19], b1, W2[64][64], b2, w3[64], b3 */
+int lb_mlp_set_params(lb_mlp *m, const float *params);  /* resets the Adam state */
+int lb_mlp_get_params(lb_mlp *m, float *params);
+/* network outputs y[n] for device rows x_dev[n][19] (the closure's forward) */
+int lb_mlp_forward(lb_mlp *m, const float *x_dev, float *y_dev, long n);
+/* gradient (host, 5505 floats) and value of the mean squared error over all n
+ * device samples */
+int lb_mlp_grad(lb_mlp *m, const float *x_dev, const float *z_dev, long n, float *grad,
+                double *loss);
+/* Adam (beta 0.9/0.999) for `steps` minibatches of `batch` contiguous samples
+ * starting at seeded random offsets; loss_log[steps] optional (host) */
+int lb_mlp_train(lb_mlp *m, const float *x_dev, const float *z_dev, long n, int steps,
+                 int batch, float lr, uint64_t seed, float *loss_log);
+/* install the closure on a D3Q19 native FP32 context (m == NULL removes it);
+ * the network must outlive its use; y_out_dev (optional, N floats) receives
+ * the raw network output of every fluid cell at each step */
+int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, float z_max,
+                      float *y_out_dev);
+/* training data from a fine lattice's last-step moment fields: Favre box
+ * filter by `factor`, features [Nc][19] and targets z = nu_t/nu0 [Nc]
+ * (device buffers; NULL to skip) and the mean resolved kinetic energy of the
+ * filtered field */
+int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
+                      float *features_dev, float *targets_dev, double *ke_mean);
+/* device pointers of a context's moment fields (valid until lb_destroy) and
+ * its extents */
+int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **uz);
+int lb_extents(const lb_ctx *ctx, int *nx, int *ny, int *nz);
+
 /* ---- device helpers (tests and hosts without their own allocator) ------ */
 int lb_device_count(int *n);
 int lb_malloc(void **ptr, size_t bytes);

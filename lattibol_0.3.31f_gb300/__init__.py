@@ -19,3 +19,4 @@ def lib():
 
 from .lattice import (DeviceData, Ensemble, Lattice, LBError, W2, W3,  # noqa: E402,F401
                       droplet_ensemble)
+from . import closure  # noqa: E402,F401

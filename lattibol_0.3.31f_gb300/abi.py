@@ -147,6 +147,23 @@ PROTOTYPES = [
     ("lb_ensemble_get_launch", _c.c_int, [_c.c_void_p, _c.c_void_p]),
     ("lb_ensemble_autotune", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p]),
     ("lb_ensemble_launch_count", _c.c_int64, [_c.c_void_p]),
+    ("lb_mlp_create", _c.c_int, [_c.c_uint64, _c.POINTER(_c.c_void_p)]),
+    ("lb_mlp_destroy", _c.c_int, [_c.c_void_p]),
+    ("lb_mlp_error", _c.c_char_p, [_c.c_void_p]),
+    ("lb_mlp_num_params", _c.c_int, []),
+    ("lb_mlp_set_params", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_mlp_get_params", _c.c_int, [_c.c_void_p, _c.c_void_p]),
+    ("lb_mlp_forward", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_long]),
+    ("lb_mlp_grad", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_long, _c.c_void_p,
+                               _c.POINTER(_c.c_double)]),
+    ("lb_mlp_train", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_long, _c.c_int,
+                                _c.c_int, _c.c_float, _c.c_uint64, _c.c_void_p]),
+    ("lb_closure_enable", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_float, _c.c_float,
+                                     _c.c_float, _c.c_void_p]),
+    ("lb_closure_sample", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_float, _c.c_float, _c.c_float,
+                                     _c.c_void_p, _c.c_void_p, _c.POINTER(_c.c_double)]),
+    ("lb_device_fields", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_void_p)] * 4),
+    ("lb_extents", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3),
     ("lb_device_count", _c.c_int, [_c.POINTER(_c.c_int)]),
     ("lb_malloc", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
     ("lb_free", _c.c_int, [_c.c_void_p]),

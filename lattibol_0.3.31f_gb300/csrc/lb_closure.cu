@@ -1,0 +1,597 @@
+// lb_closure.cu -- learned sub-grid closure for under-resolved D3Q19 flow.
+//
+// * d3q19_closure_kernel: the fused native D3Q19 step in which every cell's
+//   relaxation time comes from the closure network.  Per cell it forms 19
+//   features from the pre-collision populations -- the 18 non-conserved
+//   non-equilibrium moments (momentum 3, stress 6, third/fourth order 9 in
+//   the raw basis c_x c_y^2, ..., c_y^2 c_z^2) scaled by 1/(rho c_s^2 tau0
+//   s_ref), and |S| / s_ref with S = -Pi_neq / (2 rho c_s^2 tau0) -- and the
+//   warp evaluates the network for its 32 cells on the tensor cores.  The
+//   output y gives nu_t = nu0 * clamp(y, 0, z_max) and tau = 0.5 + 3 (nu0 +
+//   nu_t).
+// * filter / feature kernels: box-filter a fine lattice's moments onto a
+//   coarse grid (Favre averages), and from the filtered fields build the
+//   same 19 features (stress features -2 S/s_ref from central differences of
+//   the filtered velocity; the other moments are zero at first order) and
+//   the target z = nu_t/nu0 of the local least-squares eddy viscosity of the
+//   filtered sub-grid stress, nu_t = max(0, -(T_dev : S) / (2 S : S)).
+// * training: the forward pass of the closure kernel (tensor cores), an FP32
+//   backward pass per sample, per-block weight-gradient sums in shared
+//   memory, a fixed-order reduction of the block partials, and Adam.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbgb300.h"
+#include "lb_d3q19.cuh"
+
+using namespace lb;
+
+namespace lb {
+
+// ------------------------------------------------------------------ features
+// raw moment polynomials of the 18 non-conserved features
+__device__ __forceinline__ void closure_features(const float (&g)[19], float rho, float ux,
+                                                 float uy, float uz, float tau0, float s_ref,
+                                                 float (&feat)[MLP_IN]) {
+    float m[18];
+#pragma unroll
+    for (int i = 0; i < 18; i++) m[i] = 0.f;
+    const float usq = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+    for (int k = 0; k < 19; k++) {
+        const float cx = (float)d3_cx(k), cy = (float)d3_cy(k), cz = (float)d3_cz(k);
+        const float wk = k == 0 ? 1.f / 3.f : (k < 7 ? 1.f / 18.f : 1.f / 36.f);
+        const float cu = cx * ux + cy * uy + cz * uz;
+        const float feq = wk * rho * (1.f + 3.f * cu + 4.5f * cu * cu - 1.5f * usq);
+        const float fn = g[k] - feq;
+        m[0] += cx * fn;  m[1] += cy * fn;  m[2] += cz * fn;
+        m[3] += cx * cx * fn;  m[4] += cy * cy * fn;  m[5] += cz * cz * fn;
+        m[6] += cx * cy * fn;  m[7] += cx * cz * fn;  m[8] += cy * cz * fn;
+        m[9] += cx * cy * cy * fn;  m[10] += cx * cz * cz * fn;
+        m[11] += cy * cx * cx * fn; m[12] += cy * cz * cz * fn;
+        m[13] += cz * cx * cx * fn; m[14] += cz * cy * cy * fn;
+        m[15] += cx * cx * cy * cy * fn; m[16] += cx * cx * cz * cz * fn;
+        m[17] += cy * cy * cz * cz * fn;
+    }
+    const float scale = 1.f / (rho * (1.f / 3.f) * tau0 * s_ref);
+#pragma unroll
+    for (int i = 0; i < 18; i++) feat[i] = m[i] * scale;
+    // S = -Pi / (2 rho cs2 tau0): |S| = sqrt(2 S:S) with the off-diagonals twice
+    const float h = -0.5f * scale;  // S/s_ref = h * Pi
+    const float sxx = h * m[3], syy = h * m[4], szz = h * m[5];
+    const float sxy = h * m[6], sxz = h * m[7], syz = h * m[8];
+    feat[18] = sqrtf(2.f * (sxx * sxx + syy * syy + szz * szz +
+                            2.f * (sxy * sxy + sxz * sxz + syz * syz)));
+}
+
+// fused native D3Q19 step with the closure (F32 storage)
+template <bool MOM>
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
+                                                                 const ClosureArgs ca) {
+    __shared__ MlpSmemWeights sW;
+    __shared__ MlpSmemWarp sWarp[D3_BLOCK / 32];
+    mlp_load_weights(sW, ca.mlp);
+    const int lane = threadIdx.x & 31;
+    MlpSmemWarp &sw = sWarp[threadIdx.x >> 5];
+    const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
+    const int z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const bool inside = x < a.W;
+    const int o = inside ? x + a.W * (y + a.H * z) : 0;
+    const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
+    const bool fluid = !(fl & CELL_WALL);
+    float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+    float feat[MLP_IN];
+#pragma unroll
+    for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
+    if (fluid) {
+        const Nbr3 n(x, y, z, a.W, a.H, a.D);
+        pull_native<float>(a, o, n, fl, g);
+        d3q19_moments(g, rho, ux, uy, uz);
+        closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
+    }
+#pragma unroll
+    for (int i = 0; i < MLP_IN_PAD; i++)
+        sw.x[lane * SX_STRIDE + i] = __float2bfloat16_rn(i < MLP_IN ? feat[i] : 0.f);
+    __syncthreads();  // weights staged, feature rows written
+    float h2[2][8][4];
+    mlp_forward_warp(sW, sw, h2, true);
+    const float yv = sw.y[lane];
+    if (!inside) return;
+    if (!fluid) {
+        if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+        return;
+    }
+    if (ca.y_out) ca.y_out[o] = yv;
+    const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
+    const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
+    if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+    float ex = ux, ey = uy, ez = uz;
+    if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
+    if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
+    if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
+    d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+#pragma unroll
+    for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+}
+
+cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
+                                 cudaStream_t s) {
+    const dim3 g((a.W + D3_BLOCK - 1) / D3_BLOCK, a.H, a.D), b(D3_BLOCK);
+    if (mom) d3q19_closure_kernel<true><<<g, b, 0, s>>>(a, ca);
+    else d3q19_closure_kernel<false><<<g, b, 0, s>>>(a, ca);
+    return cudaGetLastError();
+}
+
+}  // namespace lb
+
+namespace {
+
+// ------------------------------------------------------------------ filter
+// Favre box filter of factor^3 fine cells onto each coarse cell: rho_bar,
+// u_bar = sum(rho u)/sum(rho), T_ab = sum(rho u_a u_b)/sum(rho) - u_a u_b.
+// out: [0] rho, [1..3] u, [4..9] T (xx, yy, zz, xy, xz, yz), each Nc floats
+__global__ void filter_kernel(const float *rho, const float *ux, const float *uy,
+                              const float *uz, int W, int H, int D, int f, float *out, long Nc) {
+    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (c >= Nc) return;
+    const int Wc = W / f, Hc = H / f;
+    const int I = (int)(c % Wc), J = (int)((c / Wc) % Hc), K = (int)(c / ((long)Wc * Hc));
+    double sr = 0, sx = 0, sy = 0, sz = 0, sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+    for (int k = 0; k < f; k++)
+        for (int j = 0; j < f; j++)
+            for (int i = 0; i < f; i++) {
+                const long o = (I * f + i) + (long)W * ((J * f + j) + (long)H * (K * f + k));
+                const double r = rho[o], vx = ux[o], vy = uy[o], vz = uz[o];
+                sr += r; sx += r * vx; sy += r * vy; sz += r * vz;
+                sxx += r * vx * vx; syy += r * vy * vy; szz += r * vz * vz;
+                sxy += r * vx * vy; sxz += r * vx * vz; syz += r * vy * vz;
+            }
+    const double bx = sx / sr, by = sy / sr, bz = sz / sr;
+    out[c] = (float)(sr / ((double)f * f * f));
+    out[Nc + c] = (float)bx;
+    out[2 * Nc + c] = (float)by;
+    out[3 * Nc + c] = (float)bz;
+    out[4 * Nc + c] = (float)(sxx / sr - bx * bx);
+    out[5 * Nc + c] = (float)(syy / sr - by * by);
+    out[6 * Nc + c] = (float)(szz / sr - bz * bz);
+    out[7 * Nc + c] = (float)(sxy / sr - bx * by);
+    out[8 * Nc + c] = (float)(sxz / sr - bx * bz);
+    out[9 * Nc + c] = (float)(syz / sr - by * bz);
+}
+
+// features and targets from the filtered fields (periodic central differences)
+__global__ void features_kernel(const float *fl, int Wc, int Hc, int Dc, float nu0, float s_ref,
+                                float z_max, float *feat, float *target) {
+    const long Nc = (long)Wc * Hc * Dc;
+    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (c >= Nc) return;
+    const int I = (int)(c % Wc), J = (int)((c / Wc) % Hc), K = (int)(c / ((long)Wc * Hc));
+    auto at = [&](int i, int j, int k) -> long {
+        i = (i + Wc) % Wc; j = (j + Hc) % Hc; k = (k + Dc) % Dc;
+        return i + (long)Wc * (j + (long)Hc * k);
+    };
+    const float *u[3] = {fl + Nc, fl + 2 * Nc, fl + 3 * Nc};
+    float du[3][3];  // du[a][b] = d u_b / d x_a
+    const long pa[3] = {at(I + 1, J, K), at(I, J + 1, K), at(I, J, K + 1)};
+    const long ma[3] = {at(I - 1, J, K), at(I, J - 1, K), at(I, J, K - 1)};
+    for (int aa = 0; aa < 3; aa++)
+        for (int b = 0; b < 3; b++) du[aa][b] = 0.5f * (u[b][pa[aa]] - u[b][ma[aa]]);
+    float S[3][3];
+    for (int aa = 0; aa < 3; aa++)
+        for (int b = 0; b < 3; b++) S[aa][b] = 0.5f * (du[aa][b] + du[b][aa]);
+    const float T[6] = {fl[4 * Nc + c], fl[5 * Nc + c], fl[6 * Nc + c],
+                        fl[7 * Nc + c], fl[8 * Nc + c], fl[9 * Nc + c]};
+    const float tr = (T[0] + T[1] + T[2]) / 3.f;
+    const float TS = (T[0] - tr) * S[0][0] + (T[1] - tr) * S[1][1] + (T[2] - tr) * S[2][2] +
+                     2.f * (T[3] * S[0][1] + T[4] * S[0][2] + T[5] * S[1][2]);
+    const float SS = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2] +
+                     2.f * (S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2]);
+    const float nut = fmaxf(0.f, -TS / (2.f * SS + 1e-30f));
+    target[c] = fminf(nut / nu0, z_max);
+    float *fo = feat + c * MLP_IN;
+    const float q = -2.f / s_ref;
+    for (int i = 0; i < MLP_IN; i++) fo[i] = 0.f;
+    fo[3] = q * S[0][0]; fo[4] = q * S[1][1]; fo[5] = q * S[2][2];
+    fo[6] = q * S[0][1]; fo[7] = q * S[0][2]; fo[8] = q * S[1][2];
+    fo[18] = sqrtf(2.f * SS) / s_ref;
+}
+
+// ------------------------------------------------------------------ training
+constexpr int HROW = MLP_H + 1;
+struct TrainSmemWarp {
+    MlpSmemWarp m;
+    float h2[32 * HROW];   // row stride 65: a warp walking its rows hits 32 banks
+    float dh2[32 * HROW];
+    float dh1[32 * HROW];
+    float dy[32];
+};
+constexpr int TRAIN_WARPS = 4;
+constexpr int NGRAD = MLP_NPARAM + 1;  // + loss
+constexpr size_t TRAIN_SMEM =
+    sizeof(MlpSmemWeights) + TRAIN_WARPS * sizeof(TrainSmemWarp) + NGRAD * sizeof(float);
+
+// forward (tensor cores, as in the closure kernel) + FP32 backward over the
+// samples [0, n) of a batch; each block leaves its gradient sums (already
+// divided by n) and its loss sum in partial[block][NGRAD]
+__global__ void __launch_bounds__(32 * TRAIN_WARPS) mlp_train_kernel(
+    MlpDev mlp, const float *X, const float *Z, long n, float *partial) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    MlpSmemWeights &sW = *reinterpret_cast<MlpSmemWeights *>(smem);
+    TrainSmemWarp *sWarp = reinterpret_cast<TrainSmemWarp *>(smem + sizeof(MlpSmemWeights));
+    float *sG = reinterpret_cast<float *>(smem + sizeof(MlpSmemWeights) +
+                                          TRAIN_WARPS * sizeof(TrainSmemWarp));
+    mlp_load_weights(sW, mlp);
+    for (int i = threadIdx.x; i < NGRAD; i += blockDim.x) sG[i] = 0.f;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    TrainSmemWarp &tw = sWarp[wid];
+    const int g = lane >> 2, t = lane & 3;
+    const float inv_n = 1.f / (float)n;
+    __syncthreads();
+    for (long base = (long)blockIdx.x * 32 * TRAIN_WARPS; base < n;
+         base += (long)gridDim.x * 32 * TRAIN_WARPS) {
+        const long s = base + wid * 32 + lane;
+        const bool valid = s < n;
+        for (int i = 0; i < MLP_IN_PAD; i++)
+            tw.m.x[lane * SX_STRIDE + i] =
+                __float2bfloat16_rn((valid && i < MLP_IN) ? X[s * MLP_IN + i] : 0.f);
+        float h2[2][8][4];
+        mlp_forward_warp(sW, tw.m, h2, true);
+        // scatter the second hidden layer to rows
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int c0 = nt * 8 + 2 * t, r0 = mt * 16 + g;
+                tw.h2[r0 * HROW + c0] = h2[mt][nt][0];
+                tw.h2[r0 * HROW + c0 + 1] = h2[mt][nt][1];
+                tw.h2[(r0 + 8) * HROW + c0] = h2[mt][nt][2];
+                tw.h2[(r0 + 8) * HROW + c0 + 1] = h2[mt][nt][3];
+            }
+        __syncwarp();
+        // per-sample backward (row = lane)
+        const float err = valid ? tw.m.y[lane] - Z[s] : 0.f;
+        const float dy = 2.f * err * inv_n;
+        tw.dy[lane] = dy;
+        float *h2r = tw.h2 + lane * HROW, *dh2r = tw.dh2 + lane * HROW;
+        for (int j = 0; j < MLP_H; j++) dh2r[j] = h2r[j] > 0.f ? dy * sW.w3[j] : 0.f;
+        float *dh1r = tw.dh1 + lane * HROW;
+        const __nv_bfloat16 *h1r = tw.m.h1 + lane * SH_STRIDE;
+        for (int i = 0; i < MLP_H; i++) {
+            float acc = 0.f;
+            if (__bfloat162float(h1r[i]) > 0.f)
+                for (int j = 0; j < MLP_H; j++)
+                    acc = acc + dh2r[j] * __bfloat162float(sW.w2[j * SW2_STRIDE + i]);
+            dh1r[i] = acc;
+        }
+        // block loss: sum over the warp, one atomic per warp into shared memory
+        float e2 = err * err;
+        for (int d = 16; d > 0; d >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, d);
+        if (lane == 0) atomicAdd(&sG[MLP_NPARAM], e2 * inv_n);
+        __syncthreads();
+        // weight gradients: every thread owns a strided subset of the parameters
+        for (int p = threadIdx.x; p < MLP_NPARAM; p += blockDim.x) {
+            float acc = 0.f;
+            for (int w = 0; w < TRAIN_WARPS; w++) {
+                const TrainSmemWarp &u = sWarp[w];
+                for (int r = 0; r < 32; r++) {
+                    float v;
+                    if (p < MLP_OFF_B1) {
+                        const int j = p / MLP_IN, f = p % MLP_IN;
+                        v = u.dh1[r * HROW + j] * __bfloat162float(u.m.x[r * SX_STRIDE + f]);
+                    } else if (p < MLP_OFF_W2) {
+                        v = u.dh1[r * HROW + (p - MLP_OFF_B1)];
+                    } else if (p < MLP_OFF_B2) {
+                        const int q = p - MLP_OFF_W2, j = q / MLP_H, i = q % MLP_H;
+                        v = u.dh2[r * HROW + j] * __bfloat162float(u.m.h1[r * SH_STRIDE + i]);
+                    } else if (p < MLP_OFF_W3) {
+                        v = u.dh2[r * HROW + (p - MLP_OFF_B2)];
+                    } else if (p < MLP_OFF_B3) {
+                        v = u.dy[r] * u.h2[r * HROW + (p - MLP_OFF_W3)];
+                    } else {
+                        v = u.dy[r];
+                    }
+                    acc = acc + v;
+                }
+            }
+            sG[p] = sG[p] + acc;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < NGRAD; i += blockDim.x) partial[(long)blockIdx.x * NGRAD + i] = sG[i];
+}
+
+__global__ void grad_reduce_kernel(const float *partial, int nblocks, float *grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NGRAD) return;
+    float s = 0.f;
+    for (int b = 0; b < nblocks; b++) s = s + partial[(long)b * NGRAD + i];
+    grad[i] = s;
+}
+
+// Adam step on the FP32 master parameters, refreshing the BF16 copies
+__global__ void adam_kernel(float *p, float *m1, float *m2, const float *grad, float lr,
+                            float b1c, float b2c, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= MLP_NPARAM) return;
+    const float gr = grad[i];
+    const float a = 0.9f * m1[i] + 0.1f * gr;
+    const float b = 0.999f * m2[i] + 0.001f * gr * gr;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = p[i] - lr * (a / b1c) / (sqrtf(b / b2c) + 1e-8f);
+    p[i] = v;
+    if (i < MLP_OFF_B1) w1b[(i / MLP_IN) * MLP_IN_PAD + i % MLP_IN] = __float2bfloat16_rn(v);
+    else if (i >= MLP_OFF_W2 && i < MLP_OFF_B2) w2b[i - MLP_OFF_W2] = __float2bfloat16_rn(v);
+}
+
+__global__ void refresh_bf16_kernel(const float *p, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < MLP_H * MLP_IN_PAD) {
+        const int j = i / MLP_IN_PAD, f = i % MLP_IN_PAD;
+        w1b[i] = __float2bfloat16_rn(f < MLP_IN ? p[MLP_OFF_W1 + j * MLP_IN + f] : 0.f);
+    }
+    if (i < MLP_H * MLP_H) w2b[i] = __float2bfloat16_rn(p[MLP_OFF_W2 + i]);
+}
+
+// inference of the network on rows of features (the closure kernel's forward)
+__global__ void __launch_bounds__(128) mlp_forward_kernel(MlpDev mlp, const float *X, long n,
+                                                          float *Y) {
+    __shared__ MlpSmemWeights sW;
+    __shared__ MlpSmemWarp sWarp[4];
+    mlp_load_weights(sW, mlp);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    MlpSmemWarp &sw = sWarp[threadIdx.x >> 5];
+    for (long base = (long)blockIdx.x * 128; base < n; base += (long)gridDim.x * 128) {
+        const long s = base + threadIdx.x;
+        for (int i = 0; i < MLP_IN_PAD; i++)
+            sw.x[lane * SX_STRIDE + i] =
+                __float2bfloat16_rn((s < n && i < MLP_IN) ? X[s * MLP_IN + i] : 0.f);
+        float h2[2][8][4];
+        mlp_forward_warp(sW, sw, h2, true);
+        if (s < n) Y[s] = sw.y[lane];
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+struct lb_mlp {
+    float *p = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *partial = nullptr;
+    __nv_bfloat16 *w1b = nullptr, *w2b = nullptr;
+    int nblocks = 304;
+    long step = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+};
+
+namespace {
+
+MlpDev mlp_dev(const lb_mlp *m) {
+    MlpDev d;
+    d.w1 = m->w1b;
+    d.w2 = m->w2b;
+    d.b1 = m->p + MLP_OFF_B1;
+    d.b2 = m->p + MLP_OFF_B2;
+    d.w3 = m->p + MLP_OFF_W3;
+    d.b3 = m->p + MLP_OFF_B3;
+    return d;
+}
+
+int mfail(lb_mlp *m, cudaError_t e, const char *where) {
+    if (m) m->err = std::string(where) + ": " + cudaGetErrorString(e);
+    return LB_ERR_CUDA;
+}
+#define LB_MTRY(m, where, call)                                   \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return mfail(m, e_, where);        \
+    } while (0)
+
+int mlp_gradient(lb_mlp *m, const float *X, const float *Z, long n) {
+    static bool attr = false;
+    if (!attr) {
+        LB_MTRY(m, "cudaFuncSetAttribute",
+                cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TRAIN_SMEM));
+        attr = true;
+    }
+    const long chunks = (n + 127) / 128;
+    const int nb = (int)std::min<long>(m->nblocks, chunks);
+    mlp_train_kernel<<<nb, 32 * TRAIN_WARPS, TRAIN_SMEM, m->stream>>>(mlp_dev(m), X, Z, n,
+                                                                      m->partial);
+    LB_MTRY(m, "mlp_train_kernel", cudaGetLastError());
+    grad_reduce_kernel<<<(NGRAD + 255) / 256, 256, 0, m->stream>>>(m->partial, nb, m->grad);
+    LB_MTRY(m, "grad_reduce_kernel", cudaGetLastError());
+    return LB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lb_mlp_create(uint64_t seed, lb_mlp **out) {
+    if (!out) return LB_ERR_ARG;
+    lb_mlp *m = new lb_mlp;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&m->p, sizeof(float) * MLP_NPARAM);
+    if (e == cudaSuccess) e = cudaMalloc(&m->m1, sizeof(float) * MLP_NPARAM);
+    if (e == cudaSuccess) e = cudaMalloc(&m->m2, sizeof(float) * MLP_NPARAM);
+    if (e == cudaSuccess) e = cudaMalloc(&m->grad, sizeof(float) * NGRAD);
+    if (e == cudaSuccess) e = cudaMalloc(&m->partial, sizeof(float) * NGRAD * m->nblocks);
+    if (e == cudaSuccess) e = cudaMalloc(&m->w1b, sizeof(__nv_bfloat16) * MLP_H * MLP_IN_PAD);
+    if (e == cudaSuccess) e = cudaMalloc(&m->w2b, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        lb_mlp_destroy(m);
+        return LB_ERR_NOMEM;
+    }
+    // He-uniform initialisation from a 64-bit LCG (host side, deterministic)
+    std::vector<float> p(MLP_NPARAM, 0.f);
+    uint64_t st = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&]() {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        return (float)((st >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f;
+    };
+    const float a1 = sqrtf(6.f / MLP_IN), a2 = sqrtf(6.f / MLP_H), a3 = sqrtf(3.f / MLP_H);
+    for (int i = 0; i < MLP_H * MLP_IN; i++) p[MLP_OFF_W1 + i] = a1 * uni();
+    for (int i = 0; i < MLP_H * MLP_H; i++) p[MLP_OFF_W2 + i] = a2 * uni();
+    for (int i = 0; i < MLP_H; i++) p[MLP_OFF_W3 + i] = a3 * uni();
+    const int rc = lb_mlp_set_params(m, p.data());
+    if (rc != LB_OK) {
+        lb_mlp_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return LB_OK;
+}
+
+int lb_mlp_destroy(lb_mlp *m) {
+    if (!m) return LB_ERR_ARG;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    cudaFree(m->p); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->partial);
+    cudaFree(m->w1b); cudaFree(m->w2b);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return LB_OK;
+}
+
+const char *lb_mlp_error(const lb_mlp *m) { return m ? m->err.c_str() : "null network"; }
+int lb_mlp_num_params(void) { return MLP_NPARAM; }
+
+int lb_mlp_set_params(lb_mlp *m, const float *p) {
+    if (!m || !p) return LB_ERR_ARG;
+    LB_MTRY(m, "set_params", cudaMemcpyAsync(m->p, p, sizeof(float) * MLP_NPARAM,
+                                             cudaMemcpyHostToDevice, m->stream));
+    LB_MTRY(m, "set_params", cudaMemsetAsync(m->m1, 0, sizeof(float) * MLP_NPARAM, m->stream));
+    LB_MTRY(m, "set_params", cudaMemsetAsync(m->m2, 0, sizeof(float) * MLP_NPARAM, m->stream));
+    refresh_bf16_kernel<<<(MLP_H * MLP_H + 255) / 256, 256, 0, m->stream>>>(m->p, m->w1b, m->w2b);
+    LB_MTRY(m, "refresh_bf16", cudaGetLastError());
+    m->step = 0;
+    LB_MTRY(m, "set_params", cudaStreamSynchronize(m->stream));
+    return LB_OK;
+}
+
+int lb_mlp_get_params(lb_mlp *m, float *p) {
+    if (!m || !p) return LB_ERR_ARG;
+    LB_MTRY(m, "get_params", cudaMemcpyAsync(p, m->p, sizeof(float) * MLP_NPARAM,
+                                             cudaMemcpyDeviceToHost, m->stream));
+    LB_MTRY(m, "get_params", cudaStreamSynchronize(m->stream));
+    return LB_OK;
+}
+
+int lb_mlp_forward(lb_mlp *m, const float *x_dev, float *y_dev, long n) {
+    if (!m || !x_dev || !y_dev || n < 0) return LB_ERR_ARG;
+    const int nb = (int)std::min<long>(1216, (n + 127) / 128);
+    if (nb > 0) mlp_forward_kernel<<<nb, 128, 0, m->stream>>>(mlp_dev(m), x_dev, n, y_dev);
+    LB_MTRY(m, "mlp_forward_kernel", cudaGetLastError());
+    LB_MTRY(m, "mlp_forward", cudaStreamSynchronize(m->stream));
+    return LB_OK;
+}
+
+int lb_mlp_grad(lb_mlp *m, const float *x_dev, const float *z_dev, long n, float *grad,
+                double *loss) {
+    if (!m || !x_dev || !z_dev || n < 1) return LB_ERR_ARG;
+    const int rc = mlp_gradient(m, x_dev, z_dev, n);
+    if (rc != LB_OK) return rc;
+    std::vector<float> h(NGRAD);
+    LB_MTRY(m, "grad", cudaMemcpyAsync(h.data(), m->grad, sizeof(float) * NGRAD,
+                                       cudaMemcpyDeviceToHost, m->stream));
+    LB_MTRY(m, "grad", cudaStreamSynchronize(m->stream));
+    if (grad) memcpy(grad, h.data(), sizeof(float) * MLP_NPARAM);
+    if (loss) *loss = h[MLP_NPARAM];
+    return LB_OK;
+}
+
+// Adam over random contiguous windows of `batch` samples (a 64-bit LCG
+// picks the window starts); loss_log[i] = loss of step i (optional)
+int lb_mlp_train(lb_mlp *m, const float *x_dev, const float *z_dev, long n, int steps,
+                 int batch, float lr, uint64_t seed, float *loss_log) {
+    if (!m || !x_dev || !z_dev || n < 1 || steps < 0 || batch < 1) return LB_ERR_ARG;
+    if (batch > n) batch = (int)n;
+    uint64_t st = seed * 2862933555777941757ULL + 3037000493ULL;
+    for (int it = 0; it < steps; it++) {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        const long start = (long)((st >> 17) % (uint64_t)(n - batch + 1));
+        int rc = mlp_gradient(m, x_dev + start * MLP_IN, z_dev + start, batch);
+        if (rc != LB_OK) return rc;
+        m->step++;
+        const float b1c = 1.f - powf(0.9f, (float)m->step), b2c = 1.f - powf(0.999f, (float)m->step);
+        adam_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, m->stream>>>(m->p, m->m1, m->m2, m->grad,
+                                                                     lr, b1c, b2c, m->w1b, m->w2b);
+        LB_MTRY(m, "adam_kernel", cudaGetLastError());
+        if (loss_log) {
+            float l;
+            LB_MTRY(m, "loss", cudaMemcpyAsync(&l, m->grad + MLP_NPARAM, sizeof(float),
+                                               cudaMemcpyDeviceToHost, m->stream));
+            LB_MTRY(m, "loss", cudaStreamSynchronize(m->stream));
+            loss_log[it] = l;
+        }
+    }
+    LB_MTRY(m, "train", cudaStreamSynchronize(m->stream));
+    return LB_OK;
+}
+
+int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, float z_max,
+                      float *y_out_dev) {
+    if (!ctx) return LB_ERR_ARG;
+    if (!m) return context_set_closure(ctx, nullptr);
+    if (!(nu0 > 0.f) || !(s_ref > 0.f) || !(z_max >= 0.f)) return LB_ERR_ARG;
+    ClosureArgs ca{};
+    ca.mlp = mlp_dev(m);
+    ca.nu0 = nu0;
+    ca.tau0 = 0.5f + 3.f * nu0;
+    ca.s_ref = s_ref;
+    ca.z_max = z_max;
+    ca.y_out = y_out_dev;
+    return context_set_closure(ctx, &ca);
+}
+
+// training data from a fine lattice: filter its last-step moment fields by
+// `factor` and write features [Nc][19] and targets [Nc] (device buffers, Nc =
+// nodes / factor^3) and the mean resolved kinetic energy of the filtered field
+int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
+                      float *features_dev, float *targets_dev, double *ke_mean) {
+    if (!fine || factor < 1) return LB_ERR_ARG;
+    float *f[4];
+    int rc = lb_device_fields(fine, &f[0], &f[1], &f[2], &f[3]);
+    if (rc != LB_OK) return rc;
+    int W, H, D;
+    rc = lb_extents(fine, &W, &H, &D);
+    if (rc != LB_OK) return rc;
+    if (W % factor || H % factor || D % factor) return LB_ERR_ARG;
+    const int Wc = W / factor, Hc = H / factor, Dc = D / factor;
+    const long Nc = (long)Wc * Hc * Dc;
+    float *fl = nullptr;
+    if (cudaMalloc(&fl, sizeof(float) * 10 * Nc) != cudaSuccess) return LB_ERR_NOMEM;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) {
+        filter_kernel<<<(unsigned)((Nc + 255) / 256), 256>>>(f[0], f[1], f[2], f[3], W, H, D,
+                                                             factor, fl, Nc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && features_dev && targets_dev) {
+        features_kernel<<<(unsigned)((Nc + 255) / 256), 256>>>(fl, Wc, Hc, Dc, nu0, s_ref, z_max,
+                                                               features_dev, targets_dev);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && ke_mean) {
+        std::vector<float> h(4 * Nc);
+        e = cudaMemcpy(h.data(), fl, sizeof(float) * 4 * Nc, cudaMemcpyDeviceToHost);
+        double ke = 0.0;
+        for (long c = 0; c < Nc; c++) {
+            const double ux = h[Nc + c], uy = h[2 * Nc + c], uz = h[3 * Nc + c];
+            ke += 0.5 * h[c] * (ux * ux + uy * uy + uz * uz);
+        }
+        *ke_mean = ke / (double)Nc;
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(fl);
+    return e == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+}
+
+}  // extern "C"

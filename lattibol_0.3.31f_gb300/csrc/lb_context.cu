@@ -31,6 +31,8 @@ struct lb_ctx {
     float corr[19] = {0};
     float wr[19] = {0};                  // 16-bit storage offsets w_k * rho_ref
     int tune = 0;                        // LB_TUNE_* bits in effect
+    bool closure_on = false;             // learned closure sets the local relaxation time
+    ClosureArgs closure{};
     bool flags_set = false;
     int64_t launches = 0;
     std::string err;
@@ -115,6 +117,10 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         if (g.mode == LB_MODE_REFERENCE) {
             c->launches += 1;
             return launch_d3q19_fused(a, MODE_REF, moments, false, c->stream);
+        }
+        if (c->closure_on) {
+            c->launches += 1;
+            return launch_d3q19_closure(a, c->closure, moments, c->stream);
         }
         const bool sc = sc_on(c);
         c->launches += sc ? 2 : 1;
@@ -468,6 +474,23 @@ int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
     return LB_OK;
 }
 
+int lb_device_fields(lb_ctx *c, float **rho, float **ux, float **uy, float **uz) {
+    if (!c) return LB_ERR_ARG;
+    if (rho) *rho = mom_k(c, 0);
+    if (ux) *ux = mom_k(c, 1);
+    if (uy) *uy = mom_k(c, 2);
+    if (uz) *uz = c->Q == 19 ? mom_k(c, 3) : nullptr;
+    return LB_OK;
+}
+
+int lb_extents(const lb_ctx *c, int *nx, int *ny, int *nz) {
+    if (!c) return LB_ERR_ARG;
+    if (nx) *nx = c->cfg.nx;
+    if (ny) *ny = c->cfg.ny;
+    if (nz) *nz = c->cfg.nz;
+    return LB_OK;
+}
+
 int lb_synchronize(lb_ctx *c) {
     if (!c) return LB_ERR_ARG;
     LB_TRY(c, "lb_synchronize", cudaStreamSynchronize(c->stream));
@@ -549,3 +572,21 @@ int lb_device_synchronize(void) {
 }
 
 }  // extern "C"
+
+// installs (ca != nullptr) or removes the learned closure of a context; the
+// closure kernel handles D3Q19 native mode with FP32 storage and no Shan-Chen
+int lb::context_set_closure(lb_ctx *c, const ClosureArgs *ca) {
+    if (!c) return LB_ERR_ARG;
+    if (ca && (c->Q != 19 || c->cfg.mode != LB_MODE_NATIVE || c->cfg.storage != LB_STORE_F32 ||
+               sc_on(c)))
+        return fail(c, LB_ERR_ARG, "closure: D3Q19 native mode, FP32 storage, no Shan-Chen");
+    LB_TRY(c, "closure", cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < 2; i++)
+        if (c->graph[i]) {
+            cudaGraphExecDestroy(c->graph[i]);
+            c->graph[i] = nullptr;
+        }
+    c->closure_on = ca != nullptr;
+    if (ca) c->closure = *ca;
+    return LB_OK;
+}

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "lb_common.cuh"
+#include "lb_mlp.cuh"
 
 namespace lb {
 
@@ -104,5 +105,21 @@ cudaError_t launch_reduce_blocks(const float *rho, const float *ux, const float 
 
 // records a message for lb_abi_last_error() on the calling thread
 void abi_record_error(const char *where, const char *what);
+
+// learned closure (lb_closure.cu): the network and its scalings
+struct ClosureArgs {
+    MlpDev mlp;
+    float nu0, tau0, s_ref, z_max;
+    float *y_out;  // optional: network output per cell (tests)
+};
+cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
+                                 cudaStream_t s);
+
+}  // namespace lb
+
+struct lb_ctx;
+namespace lb {
+// installs (ca != nullptr) or removes the closure of a context (lb_context.cu)
+int context_set_closure(lb_ctx *c, const ClosureArgs *ca);
 
 }  // namespace lb

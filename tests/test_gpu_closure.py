@@ -1,0 +1,184 @@
+"""GPU checks of the learned closure: the tensor-core network against the
+numpy oracle (forward and gradient), training, the closure kernel's features
+and its fallback behaviour, the filter/feature kernels, and a small
+Taylor-Green case showing what the trained closure gains over plain coarse
+BGK."""
+import ctypes
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ORACLE_DIR, load_package
+from golden_io import bits
+
+pytestmark = pytest.mark.gpu
+sys.path.insert(0, ORACLE_DIR)
+import mlp_oracle  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    p = load_package()
+    n = ctypes.c_int(0)
+    assert p.lib().lb_device_count(ctypes.byref(n)) == 0 and n.value >= 1, "no CUDA device"
+    return p
+
+
+def test_mlp_forward_matches_oracle(pkg):
+    net = pkg.closure.Mlp(seed=3)
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((1000, 19)).astype(np.float32)
+    y = net.forward(X)
+    ref = mlp_oracle.forward(net.params(), X)["y"]
+    # FP32 accumulation order only (identical bf16 rounding points)
+    np.testing.assert_allclose(y, ref, rtol=2e-3, atol=2e-3 * np.abs(ref).max())
+    net.close()
+
+
+def test_mlp_gradient_matches_oracle(pkg):
+    net = pkg.closure.Mlp(seed=5)
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((777, 19)).astype(np.float32)  # not a multiple of 128
+    Z = rng.standard_normal(777).astype(np.float32)
+    g, loss = net.grad(X, Z)
+    g_ref, loss_ref = mlp_oracle.grad(net.params(), X, Z)
+    assert abs(loss - loss_ref) <= 1e-4 * abs(loss_ref)
+    assert np.linalg.norm(g - g_ref) <= 2e-3 * np.linalg.norm(g_ref)
+    for a, b in [(mlp_oracle.OFF_W1, mlp_oracle.OFF_B1), (mlp_oracle.OFF_W2, mlp_oracle.OFF_B2),
+                 (mlp_oracle.OFF_W3, mlp_oracle.OFF_B3)]:
+        assert np.linalg.norm(g[a:b] - g_ref[a:b]) <= 5e-3 * np.linalg.norm(g_ref[a:b])
+    net.close()
+
+
+def test_mlp_training_reduces_loss(pkg):
+    C = pkg.closure
+    net = C.Mlp(seed=9)
+    rng = np.random.default_rng(2)
+    n = 40000
+    X = rng.standard_normal((n, 19)).astype(np.float32)
+    Z = (2 * np.abs(X[:, 18]) + np.maximum(X[:, 3], 0) - 0.5 * X[:, 6] ** 2).astype(np.float32)
+    dx, dz = C.DeviceArray(n * 19), C.DeviceArray(n)
+    dx.upload(X)
+    dz.upload(Z)
+    log = net.train_device(dx, dz, n, steps=400, batch=2048, lr=3e-3)
+    assert np.isfinite(log).all()
+    assert np.mean(log[-20:]) < 0.1 * np.mean(log[:5])
+    net.close()
+
+
+def _tgv_lattice(pkg, n, tau_inv):
+    lat = pkg.Lattice(19, n, n, n, tau_inv=tau_inv)
+    lat.set_flags(np.zeros(n ** 3, np.uint8))
+    lat.init_equilibrium(*pkg.closure.tgv_fields(n, 0.05))
+    return lat
+
+
+def test_closure_constant_network_is_bgk(pkg):
+    """A network with constant output c relaxes every cell with tau = 0.5 +
+    3 nu0 (1 + c): bit-identical to plain BGK at that tau."""
+    C = pkg.closure
+    n, nu0, c = 24, np.float32(0.002), np.float32(0.75)
+    net = C.Mlp(seed=1)
+    p = np.zeros(net.nparam, np.float32)
+    p[-1] = c
+    net.set_params(p)
+    f32 = np.float32
+    tau_inv = f32(1) / (f32(0.5) + f32(3) * (nu0 + nu0 * c))
+    a = _tgv_lattice(pkg, n, tau_inv)
+    b = _tgv_lattice(pkg, n, f32(1.0))
+    L = pkg.lib()
+    assert L.lb_closure_enable(b.h, net.h, nu0, f32(0.01), f32(100.0), None) == 0
+    a.step(20)
+    b.step(20)
+    assert np.array_equal(bits(a.populations()), bits(b.populations()))
+    a.close()
+    b.close()
+    net.close()
+
+
+def test_closure_kernel_features_and_output(pkg, oracle):
+    """The per-cell network output of the closure kernel equals the oracle's
+    network on the oracle's features of the same pre-collision populations
+    (tolerance: the kernel forms features in FP32 before the BF16 rounding)."""
+    C = pkg.closure
+    n = 24
+    N = n ** 3
+    net = C.Mlp(seed=11)
+    nu0, s_ref = 0.003, 0.05 * 2 * np.pi / n
+    rng = np.random.default_rng(4)
+    rho, ux, uy, uz = C.tgv_fields(n, 0.05)
+    ux = (ux + 0.01 * rng.standard_normal(N)).astype(np.float32)
+    f0 = oracle.d3q19_equilibrium(rho, ux, uy, uz, *pkg.W3)
+    f0 = (f0 * (1 + 0.002 * rng.standard_normal(f0.shape))).astype(np.float32)
+    lat = pkg.Lattice(19, n, n, n, tau_inv=1.0)
+    lat.set_flags(np.zeros(N, np.uint8))
+    lat.set_populations(f0)
+    yd = C.DeviceArray(N)
+    L = pkg.lib()
+    assert L.lb_closure_enable(lat.h, net.h, np.float32(nu0), np.float32(s_ref),
+                               np.float32(50.0), yd.ptr) == 0
+    lat.step(1)
+    y = yd.download()
+    f = f0.copy()
+    oracle.d3q19_stream_native(f, np.zeros(N, np.uint8), np.zeros(19, np.float32), n, n, n)
+    g = f[oracle.D3_OPP]  # natural slot order after the swap streaming
+    F = mlp_oracle.cell_features(g, 0.5 + 3 * nu0, s_ref)
+    y_ref = mlp_oracle.forward(net.params(), F.astype(np.float32))["y"]
+    np.testing.assert_allclose(y, y_ref, rtol=3e-2, atol=3e-2 * np.abs(y_ref).max())
+    lat.close()
+    net.close()
+
+
+def test_closure_sample_matches_oracle(pkg):
+    """Favre box filter, features and targets of lb_closure_sample against
+    numpy on the same fine moment fields."""
+    C = pkg.closure
+    n, fac = 32, 4
+    fr = C.FineRun(n, fac, 0.05, 400.0)
+    fr.advance(30)
+    nc3 = (n // fac) ** 3
+    feat, targ = C.DeviceArray(nc3 * 19), C.DeviceArray(nc3)
+    ke = fr.sample(feat, targ)
+    rho, ux, uy, uz = fr.lat.moments()
+    r, ub, T = mlp_oracle.box_filter(rho, ux, uy, uz, n, n, n, fac)
+    F, z = mlp_oracle.features_targets(ub, T, fr.nu_c, fr.s_ref, fr.z_max)
+    np.testing.assert_allclose(feat.download().reshape(-1, 19), F, rtol=1e-3, atol=1e-5)
+    np.testing.assert_allclose(targ.download(), z, rtol=1e-2, atol=1e-3)
+    ke_ref = float(np.mean(0.5 * r * (ub[0] ** 2 + ub[1] ** 2 + ub[2] ** 2)))
+    assert abs(ke - ke_ref) <= 1e-5 * ke_ref
+    fr.close()
+
+
+def test_closure_gain_over_plain_coarse_bgk(pkg):
+    """Taylor-Green at Re = 200 on 64^3 (tau 0.5076), filtered by 4 onto 16^3
+    (tau 0.5019): the closure trained on the filtered fine run tracks the
+    filtered kinetic-energy decay better than plain coarse BGK over 10
+    convective times."""
+    C = pkg.closure
+    U0, Re, nf, fac = 0.05, 200.0, 64, 4
+    nc = nf // fac
+    every_c = 16
+    fr = C.FineRun(nf, fac, U0, Re)
+    L_c = nc / (2 * np.pi)
+    steps_c = int(round(10 * L_c / U0))
+    nsamp = steps_c // every_c
+    feat, targ = C.DeviceArray((nsamp + 1) * nc ** 3 * 19), C.DeviceArray((nsamp + 1) * nc ** 3)
+    ke_ref = [fr.sample(feat, targ, 0)]
+    for i in range(1, nsamp + 1):
+        fr.advance(every_c * fac)
+        ke_ref.append(fr.sample(feat, targ, i * nc ** 3))
+    fr.close()
+    ntrain = (nsamp + 1) * nc ** 3
+    net = C.Mlp(seed=2)
+    log = net.train_device(feat, targ, ntrain, steps=600, batch=4096, lr=2e-3)
+    assert np.isfinite(log).all()
+    ke_plain, _ = C.coarse_run(nc, U0, Re, nsamp * every_c, every_c)
+    ke_learn, _ = C.coarse_run(nc, U0, Re, nsamp * every_c, every_c, mlp=net)
+    e_plain = C.ke_error(ke_plain, ke_ref)
+    e_learn = C.ke_error(ke_learn, ke_ref)
+    print("CLOSURE_GAIN Re=%g %d^3->%d^3: KE error plain=%.4g learned=%.4g final loss=%.4g"
+          % (Re, nf, nc, e_plain, e_learn, float(np.mean(log[-20:]))))
+    assert np.isfinite(e_learn)
+    assert e_learn < e_plain
+    net.close()
