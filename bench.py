@@ -174,6 +174,89 @@ def run_ensemble(args, dist, ws, rank, local):
     return 0
 
 
+CLOSURE = {"U0": 0.05, "Re": 1600.0, "fine": 512, "factor": 4, "t_end": 10.0,
+           "ke_every_coarse": 64, "train_snapshots": 16, "train_steps": 3000,
+           "batch": 16384, "lr": 2e-3}
+
+
+def run_closure(args, dist, ws, rank, local):
+    """Learned closure for the under-resolved Taylor-Green vortex (Re 1600,
+    U0 = 0.05): fine 512^3 FP32 BGK run, Favre box filter by 4 onto 128^3
+    (training data at 16 snapshots, filtered kinetic energy every 64 coarse
+    steps), GPU training of the closure network, then 128^3 coarse runs with
+    plain BGK (the fallback) and with the closure over 10 convective times.
+    value = wall time of the fine run / wall time of the closure run, with the
+    kinetic-energy decay error of both coarse runs against the filtered fine
+    run."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.closure
+    cfg = dict(CLOSURE)
+    if args.size:
+        cfg["fine"] = args.size[0]
+    nf, fac, U0, Re = cfg["fine"], cfg["factor"], cfg["U0"], cfg["Re"]
+    nc = nf // fac
+    steps_c = int(round(cfg["t_end"] * (nc / (2 * np.pi)) / U0))
+    every = cfg["ke_every_coarse"]
+    nsamp = steps_c // every
+    train_at = set(np.linspace(0, nsamp, cfg["train_snapshots"]).astype(int).tolist())
+    fr = C.FineRun(nf, fac, U0, Re)
+    feat = C.DeviceArray(len(train_at) * nc ** 3 * 19)
+    targ = C.DeviceArray(len(train_at) * nc ** 3)
+    slot = 0
+    ke_ref = []
+    for i in range(nsamp + 1):
+        if i:
+            fr.advance(every * fac)
+        if i in train_at:
+            ke_ref.append(fr.sample(feat, targ, slot * nc ** 3))
+            slot += 1
+        else:
+            ke_ref.append(fr.sample())
+    fine_seconds, fine_steps = fr.seconds, fr.steps
+    fr.close()
+    net = C.Mlp(seed=2)
+    t0 = time.perf_counter()
+    log = net.train_device(feat, targ, slot * nc ** 3, steps=cfg["train_steps"],
+                           batch=cfg["batch"], lr=cfg["lr"])
+    train_seconds = time.perf_counter() - t0
+    feat.free()
+    targ.free()
+    ke_plain, plain_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every)
+    with ClockSampler(local) as clk:
+        ke_learn, learn_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every, mlp=net)
+    net.close()
+    e_plain, e_learn = C.ke_error(ke_plain, ke_ref), C.ke_error(ke_learn, ke_ref)
+    if rank != 0:
+        return 0
+    plain_blowup = None
+    if not np.all(np.isfinite(ke_plain)):
+        plain_blowup = int(np.argmax(~np.isfinite(ke_plain)) * every)
+    line = {"metric": "closure_speedup_at_ke_error", "value": fine_seconds / learn_seconds,
+            "unit": "x", "n_gpus": ws, "steps": nsamp * every, "warmup": 0,
+            "ms_per_step": 1e3 * learn_seconds / (nsamp * every), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
+            "config": {"workload": "closure_tgv_re1600_%d_to_%d" % (nf, nc), "U0": U0, "Re": Re,
+                       "fine_nodes": nf ** 3, "coarse_nodes": nc ** 3, "filter": "Favre box %d^3"
+                       % fac, "convective_times": cfg["t_end"],
+                       "mlp": "19-64-64-1 ReLU, BF16 tensor cores, FP32 accumulate",
+                       "training": {"snapshots": slot, "samples": slot * nc ** 3,
+                                    "adam_steps": cfg["train_steps"], "batch": cfg["batch"],
+                                    "final_loss": float(np.mean(log[-20:]))}},
+            "closure": {"ke_error_learned": e_learn, "ke_error_plain": e_plain,
+                        "plain_blowup_step": plain_blowup, "fine_seconds": fine_seconds,
+                        "fine_steps": fine_steps, "coarse_closure_seconds": learn_seconds,
+                        "coarse_plain_seconds": plain_seconds, "train_seconds": train_seconds,
+                        "coarse_closure_glups": nc ** 3 * nsamp * every / learn_seconds / 1e9,
+                        "fine_glups": nf ** 3 * fine_steps / fine_seconds / 1e9,
+                        "ke_curve_stride_coarse_steps": every,
+                        "ke_ref": [round(v / ke_ref[0], 5) for v in ke_ref[::4]],
+                        "ke_learned": [round(float(v / ke_learn[0]), 5) for v in ke_learn[::4]]},
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -328,7 +411,8 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="channel", choices=sorted(WORKLOADS) + ["ensemble"])
+    ap.add_argument("--workload", default="channel",
+                    choices=sorted(WORKLOADS) + ["ensemble", "closure"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--tuning", type=lambda v: int(v, 0), default=0,
@@ -337,13 +421,14 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()
-    if args.workload == "ensemble":
+    if args.workload in ("ensemble", "closure"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the CPU leg is measured on "
                               "the channel workload only"}))
             return 0
         ws, rank, local = dist_env()
-        return run_ensemble(args, dist_init(ws, "gloo"), ws, rank, local)
+        run = run_ensemble if args.workload == "ensemble" else run_closure
+        return run(args, dist_init(ws, "gloo"), ws, rank, local)
     wl = WORKLOADS[args.workload]
     if args.size:
         wl.size = tuple(args.size)

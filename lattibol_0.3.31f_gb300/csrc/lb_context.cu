@@ -199,8 +199,12 @@ void prepare_flags(const lb_ctx *c, const uint8_t *in, std::vector<uint8_t> &fla
                 }
         return;
     }
-    for (long o = 0; o < N; o++)
+    bool any_wall = false;
+    for (long o = 0; o < N; o++) {
         flags[o] = (in[o] & CELL_WALL) ? (in[o] & (CELL_WALL | CELL_MOVING)) : 0;
+        any_wall = any_wall || flags[o];
+    }
+    if (!any_wall) return;  // fully periodic: no fluid cell is near a wall
     for (int z = 0; z < D; z++)
         for (int y = 0; y < H; y++)
             for (int x = 0; x < W; x++) {

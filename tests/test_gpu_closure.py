@@ -150,13 +150,14 @@ def test_closure_sample_matches_oracle(pkg):
     fr.close()
 
 
-def test_closure_gain_over_plain_coarse_bgk(pkg):
-    """Taylor-Green at Re = 200 on 64^3 (tau 0.5076), filtered by 4 onto 16^3
-    (tau 0.5019): the closure trained on the filtered fine run tracks the
-    filtered kinetic-energy decay better than plain coarse BGK over 10
-    convective times."""
+@pytest.mark.parametrize("Re,nf", [(800.0, 64), (1600.0, 128)], ids=["Re800", "Re1600"])
+def test_closure_gain_over_plain_coarse_bgk(pkg, Re, nf):
+    """Taylor-Green filtered by 4 onto a coarse grid, 10 convective times: the
+    closure trained on the filtered fine run tracks the filtered
+    kinetic-energy decay at least twice as well as plain coarse BGK (which at
+    Re 1600 on 32^3 does not survive: infinite error)."""
     C = pkg.closure
-    U0, Re, nf, fac = 0.05, 200.0, 64, 4
+    U0, fac = 0.05, 4
     nc = nf // fac
     every_c = 16
     fr = C.FineRun(nf, fac, U0, Re)
@@ -179,6 +180,6 @@ def test_closure_gain_over_plain_coarse_bgk(pkg):
     e_learn = C.ke_error(ke_learn, ke_ref)
     print("CLOSURE_GAIN Re=%g %d^3->%d^3: KE error plain=%.4g learned=%.4g final loss=%.4g"
           % (Re, nf, nc, e_plain, e_learn, float(np.mean(log[-20:]))))
-    assert np.isfinite(e_learn)
-    assert e_learn < e_plain
+    assert np.isfinite(e_learn) and e_learn < 0.15
+    assert e_learn < 0.5 * e_plain
     net.close()
