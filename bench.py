@@ -133,7 +133,8 @@ def run_ensemble(args, dist, ws, rank, local):
     GLUPS counts the nodes of all domains."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
-    nx, ny, G, rho = pkg.droplet_ensemble(ENSEMBLE["domains"], seed=ENSEMBLE["seed"])
+    nx, ny, G, rho = pkg.droplet_ensemble(args.domains or ENSEMBLE["domains"],
+                                          seed=ENSEMBLE["seed"])
     steps = args.steps if args.steps else ENSEMBLE["steps"]
     ens = pkg.Ensemble(nx, ny, G)
     shape = ens.autotune(trial_steps=3)
@@ -418,6 +419,8 @@ def main():
     ap.add_argument("--tuning", type=lambda v: int(v, 0), default=0,
                     help="lb_config.tuning (0 = the library's default)")
     ap.add_argument("--graph-steps", type=int, default=64)
+    ap.add_argument("--domains", type=int, default=None,
+                    help="ensemble: number of domains (profiling of a smaller case only)")
     ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()
