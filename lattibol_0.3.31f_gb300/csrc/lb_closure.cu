@@ -35,25 +35,30 @@ namespace lb {
 __device__ __forceinline__ void closure_features(const float (&g)[19], float rho, float ux,
                                                  float uy, float uz, float tau0, float s_ref,
                                                  float (&feat)[MLP_IN]) {
+    // the lattice coefficients are 0 or +-1 and known at compile time after
+    // unrolling; terms with a zero coefficient are skipped explicitly (a float
+    // multiply by 0 could not be folded away)
     float m[18];
 #pragma unroll
     for (int i = 0; i < 18; i++) m[i] = 0.f;
     const float usq = ux * ux + uy * uy + uz * uz;
+    auto addc = [](float acc, int c, float v) { return c > 0 ? acc + v : (c < 0 ? acc - v : acc); };
 #pragma unroll
     for (int k = 0; k < 19; k++) {
-        const float cx = (float)d3_cx(k), cy = (float)d3_cy(k), cz = (float)d3_cz(k);
+        const int cx = d3_cx(k), cy = d3_cy(k), cz = d3_cz(k);
         const float wk = k == 0 ? 1.f / 3.f : (k < 7 ? 1.f / 18.f : 1.f / 36.f);
-        const float cu = cx * ux + cy * uy + cz * uz;
+        const float cu = addc(addc(addc(0.f, cx, ux), cy, uy), cz, uz);
         const float feq = wk * rho * (1.f + 3.f * cu + 4.5f * cu * cu - 1.5f * usq);
         const float fn = g[k] - feq;
-        m[0] += cx * fn;  m[1] += cy * fn;  m[2] += cz * fn;
-        m[3] += cx * cx * fn;  m[4] += cy * cy * fn;  m[5] += cz * cz * fn;
-        m[6] += cx * cy * fn;  m[7] += cx * cz * fn;  m[8] += cy * cz * fn;
-        m[9] += cx * cy * cy * fn;  m[10] += cx * cz * cz * fn;
-        m[11] += cy * cx * cx * fn; m[12] += cy * cz * cz * fn;
-        m[13] += cz * cx * cx * fn; m[14] += cz * cy * cy * fn;
-        m[15] += cx * cx * cy * cy * fn; m[16] += cx * cx * cz * cz * fn;
-        m[17] += cy * cy * cz * cz * fn;
+        m[0] = addc(m[0], cx, fn);  m[1] = addc(m[1], cy, fn);  m[2] = addc(m[2], cz, fn);
+        m[3] = addc(m[3], cx * cx, fn);  m[4] = addc(m[4], cy * cy, fn);
+        m[5] = addc(m[5], cz * cz, fn);  m[6] = addc(m[6], cx * cy, fn);
+        m[7] = addc(m[7], cx * cz, fn);  m[8] = addc(m[8], cy * cz, fn);
+        m[9] = addc(m[9], cx * cy * cy, fn);   m[10] = addc(m[10], cx * cz * cz, fn);
+        m[11] = addc(m[11], cy * cx * cx, fn); m[12] = addc(m[12], cy * cz * cz, fn);
+        m[13] = addc(m[13], cz * cx * cx, fn); m[14] = addc(m[14], cz * cy * cy, fn);
+        m[15] = addc(m[15], cx * cx * cy * cy, fn); m[16] = addc(m[16], cx * cx * cz * cz, fn);
+        m[17] = addc(m[17], cy * cy * cz * cz, fn);
     }
     const float scale = 1.f / (rho * (1.f / 3.f) * tau0 * s_ref);
 #pragma unroll
@@ -67,62 +72,80 @@ __device__ __forceinline__ void closure_features(const float (&g)[19], float rho
 }
 
 // fused native D3Q19 step with the closure (F32 storage)
+// Persistent: each block stages the network once and then walks row-blocks
+// of D3_BLOCK cells (x-run at fixed y, z) with a stride of the grid size.
 template <bool MOM>
 __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
                                                                  const ClosureArgs ca) {
     __shared__ MlpSmemWeights sW;
     __shared__ MlpSmemWarp sWarp[D3_BLOCK / 32];
     mlp_load_weights(sW, ca.mlp);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     MlpSmemWarp &sw = sWarp[threadIdx.x >> 5];
-    const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
-    const int x = bx * blockDim.x + threadIdx.x;
-    const int y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
-    const int z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
-    const bool inside = x < a.W;
-    const int o = inside ? x + a.W * (y + a.H * z) : 0;
-    const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
-    const bool fluid = !(fl & CELL_WALL);
-    float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
-    float feat[MLP_IN];
+    const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
+    const long nrows = (long)nbx * a.H * a.D;
+    for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
+        const long rr = a.reverse ? nrows - 1 - r : r;
+        const int bx = (int)(rr % nbx);
+        const long yz = rr / nbx;
+        const int y = (int)(yz % a.H), z = (int)(yz / a.H);
+        const int x = bx * D3_BLOCK + threadIdx.x;
+        const bool inside = x < a.W;
+        const int o = inside ? x + a.W * (y + a.H * z) : 0;
+        const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
+        const bool fluid = !(fl & CELL_WALL);
+        float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        float feat[MLP_IN];
 #pragma unroll
-    for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
-    if (fluid) {
-        const Nbr3 n(x, y, z, a.W, a.H, a.D);
-        pull_native<float>(a, o, n, fl, g);
-        d3q19_moments(g, rho, ux, uy, uz);
-        closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
+        for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
+        if (fluid) {
+            const Nbr3 n(x, y, z, a.W, a.H, a.D);
+            pull_native<float>(a, o, n, fl, g);
+            d3q19_moments(g, rho, ux, uy, uz);
+            closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
+        }
+        __nv_bfloat162 *row = reinterpret_cast<__nv_bfloat162 *>(sw.x + lane * SX_STRIDE);
+#pragma unroll
+        for (int i = 0; i < MLP_IN_PAD / 2; i++)
+            row[i] = __floats2bfloat162_rn(2 * i < MLP_IN ? feat[2 * i] : 0.f,
+                                           2 * i + 1 < MLP_IN ? feat[2 * i + 1] : 0.f);
+        mlp_output_warp(sW, sw);
+        const float yv = sw.y[lane];
+        if (!inside) continue;
+        if (!fluid) {
+            if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+            continue;
+        }
+        if (ca.y_out) ca.y_out[o] = yv;
+        const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
+        const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
+        if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+        float ex = ux, ey = uy, ez = uz;
+        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
+        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
+        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
+        d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+#pragma unroll
+        for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
     }
-#pragma unroll
-    for (int i = 0; i < MLP_IN_PAD; i++)
-        sw.x[lane * SX_STRIDE + i] = __float2bfloat16_rn(i < MLP_IN ? feat[i] : 0.f);
-    __syncthreads();  // weights staged, feature rows written
-    float h2[2][8][4];
-    mlp_forward_warp(sW, sw, h2, true);
-    const float yv = sw.y[lane];
-    if (!inside) return;
-    if (!fluid) {
-        if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
-        return;
-    }
-    if (ca.y_out) ca.y_out[o] = yv;
-    const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
-    const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
-    if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
-    float ex = ux, ey = uy, ez = uz;
-    if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
-    if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
-    if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
-    d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
-#pragma unroll
-    for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
 }
 
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s) {
-    const dim3 g((a.W + D3_BLOCK - 1) / D3_BLOCK, a.H, a.D), b(D3_BLOCK);
-    if (mom) d3q19_closure_kernel<true><<<g, b, 0, s>>>(a, ca);
-    else d3q19_closure_kernel<false><<<g, b, 0, s>>>(a, ca);
+    static int grid_cap = 0;  // SMs x resident blocks of the kernel, computed once
+    if (!grid_cap) {
+        int dev = 0, sms = 1, occ = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, d3q19_closure_kernel<false>,
+                                                      D3_BLOCK, 0);
+        grid_cap = sms * (occ > 0 ? occ : 1);
+    }
+    const long nrows = (long)((a.W + D3_BLOCK - 1) / D3_BLOCK) * a.H * a.D;
+    const unsigned g = (unsigned)(nrows < grid_cap ? nrows : grid_cap);
+    if (mom) d3q19_closure_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
+    else d3q19_closure_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
     return cudaGetLastError();
 }
 

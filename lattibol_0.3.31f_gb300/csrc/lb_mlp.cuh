@@ -85,18 +85,16 @@ __device__ __forceinline__ void mlp_load_weights(MlpSmemWeights &s, const MlpDev
     if (threadIdx.x == 0 && threadIdx.y == 0) s.b3 = m.b3[0];
 }
 
-// One warp, 32 samples: lane r has written its (padded) input row r into
-// sw.x.  Computes the first hidden layer into sw.h1 (BF16, after ReLU) and
-// returns in h2[nt][j] this lane's C-fragment values of the second hidden
-// layer (after ReLU, FP32) for both m-tiles: h2[mt][nt][j].  Optionally
-// writes the network output y of every row into sw.y.
-__device__ __forceinline__ void mlp_forward_warp(const MlpSmemWeights &s, MlpSmemWarp &sw,
-                                                 float (&h2)[2][8][4], bool want_y) {
+// One warp, rows 16*mt .. 16*mt+15 of its 32 samples (the input rows are in
+// sw.x, written and __syncwarp'ed by the caller).  Writes those rows of the
+// first hidden layer into sw.h1 (BF16, after ReLU), returns this lane's
+// C-fragment values of the second hidden layer (after ReLU, FP32) in
+// h2[nt][j], and -- if want_y -- the network output of the 16 rows in sw.y.
+// One m-tile at a time keeps 32 accumulators live instead of 64.
+__device__ __forceinline__ void mlp_forward_tile(const MlpSmemWeights &s, MlpSmemWarp &sw,
+                                                 int mt, float (&h2)[8][4], bool want_y) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __syncwarp();
-    // layer 1: [32 x 32] x [32 x 64]
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
+    {
         float acc[8][4];
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
@@ -115,64 +113,73 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmemWeights &s, MlpSme
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
             const int c0 = nt * 8 + 2 * t, r0 = mt * 16 + g;
-            sw.h1[r0 * SH_STRIDE + c0] = __float2bfloat16_rn(fmaxf(acc[nt][0] + s.b1[c0], 0.f));
-            sw.h1[r0 * SH_STRIDE + c0 + 1] =
-                __float2bfloat16_rn(fmaxf(acc[nt][1] + s.b1[c0 + 1], 0.f));
-            sw.h1[(r0 + 8) * SH_STRIDE + c0] =
-                __float2bfloat16_rn(fmaxf(acc[nt][2] + s.b1[c0], 0.f));
-            sw.h1[(r0 + 8) * SH_STRIDE + c0 + 1] =
-                __float2bfloat16_rn(fmaxf(acc[nt][3] + s.b1[c0 + 1], 0.f));
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(fmaxf(acc[nt][0] + s.b1[c0], 0.f),
+                                                            fmaxf(acc[nt][1] + s.b1[c0 + 1], 0.f));
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(fmaxf(acc[nt][2] + s.b1[c0], 0.f),
+                                                            fmaxf(acc[nt][3] + s.b1[c0 + 1], 0.f));
+            *reinterpret_cast<__nv_bfloat162 *>(sw.h1 + r0 * SH_STRIDE + c0) = lo;
+            *reinterpret_cast<__nv_bfloat162 *>(sw.h1 + (r0 + 8) * SH_STRIDE + c0) = hi;
         }
     }
     __syncwarp();
-    // layer 2: [32 x 64] x [64 x 64]
 #pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
+    for (int nt = 0; nt < 8; nt++) h2[nt][0] = h2[nt][1] = h2[nt][2] = h2[nt][3] = 0.f;
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++)
-            h2[mt][nt][0] = h2[mt][nt][1] = h2[mt][nt][2] = h2[mt][nt][3] = 0.f;
-#pragma unroll
-        for (int kt = 0; kt < 4; kt++) {
-            const __nv_bfloat16 *ha = sw.h1 + (mt * 16 + g) * SH_STRIDE + kt * 16 + 2 * t;
-            const uint32_t a[4] = {ld_b32(ha), ld_b32(ha + 8 * SH_STRIDE), ld_b32(ha + 8),
-                                   ld_b32(ha + 8 * SH_STRIDE + 8)};
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const __nv_bfloat16 *wb = s.w2 + (nt * 8 + g) * SW2_STRIDE + kt * 16 + 2 * t;
-                const uint32_t b[2] = {ld_b32(wb), ld_b32(wb + 8)};
-                mma_bf16_16816(h2[mt][nt], a, b);
-            }
-        }
+    for (int kt = 0; kt < 4; kt++) {
+        const __nv_bfloat16 *ha = sw.h1 + (mt * 16 + g) * SH_STRIDE + kt * 16 + 2 * t;
+        const uint32_t a[4] = {ld_b32(ha), ld_b32(ha + 8 * SH_STRIDE), ld_b32(ha + 8),
+                               ld_b32(ha + 8 * SH_STRIDE + 8)};
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
-            const int c0 = nt * 8 + 2 * t;
-            h2[mt][nt][0] = fmaxf(h2[mt][nt][0] + s.b2[c0], 0.f);
-            h2[mt][nt][1] = fmaxf(h2[mt][nt][1] + s.b2[c0 + 1], 0.f);
-            h2[mt][nt][2] = fmaxf(h2[mt][nt][2] + s.b2[c0], 0.f);
-            h2[mt][nt][3] = fmaxf(h2[mt][nt][3] + s.b2[c0 + 1], 0.f);
+            const __nv_bfloat16 *wb = s.w2 + (nt * 8 + g) * SW2_STRIDE + kt * 16 + 2 * t;
+            const uint32_t b[2] = {ld_b32(wb), ld_b32(wb + 8)};
+            mma_bf16_16816(h2[nt], a, b);
         }
     }
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const int c0 = nt * 8 + 2 * t;
+        h2[nt][0] = fmaxf(h2[nt][0] + s.b2[c0], 0.f);
+        h2[nt][1] = fmaxf(h2[nt][1] + s.b2[c0 + 1], 0.f);
+        h2[nt][2] = fmaxf(h2[nt][2] + s.b2[c0], 0.f);
+        h2[nt][3] = fmaxf(h2[nt][3] + s.b2[c0 + 1], 0.f);
+    }
     if (!want_y) return;
-    // output layer: per row, sum over the 64 columns held by the 4 lanes of a group
+    float p0 = 0.f, p1 = 0.f;  // rows mt*16+g and mt*16+g+8
 #pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const int c0 = nt * 8 + 2 * t;
+        p0 = p0 + h2[nt][0] * s.w3[c0];
+        p0 = p0 + h2[nt][1] * s.w3[c0 + 1];
+        p1 = p1 + h2[nt][2] * s.w3[c0];
+        p1 = p1 + h2[nt][3] * s.w3[c0 + 1];
+    }
+    p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, 1);
+    p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, 2);
+    p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, 1);
+    p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, 2);
+    if (t == 0) {
+        sw.y[mt * 16 + g] = p0 + s.b3;
+        sw.y[mt * 16 + g + 8] = p1 + s.b3;
+    }
+}
+
+// The whole warp tile (32 rows): h2 of both m-tiles and, if want_y, sw.y.
+__device__ __forceinline__ void mlp_forward_warp(const MlpSmemWeights &s, MlpSmemWarp &sw,
+                                                 float (&h2)[2][8][4], bool want_y) {
+    __syncwarp();
+    mlp_forward_tile(s, sw, 0, h2[0], want_y);
+    mlp_forward_tile(s, sw, 1, h2[1], want_y);
+    __syncwarp();
+}
+
+// Only the outputs: sw.y for the 32 rows, one m-tile at a time.
+__device__ __forceinline__ void mlp_output_warp(const MlpSmemWeights &s, MlpSmemWarp &sw) {
+    __syncwarp();
+#pragma unroll 1
     for (int mt = 0; mt < 2; mt++) {
-        float p0 = 0.f, p1 = 0.f;  // rows mt*16+g and mt*16+g+8
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const int c0 = nt * 8 + 2 * t;
-            p0 = p0 + h2[mt][nt][0] * s.w3[c0];
-            p0 = p0 + h2[mt][nt][1] * s.w3[c0 + 1];
-            p1 = p1 + h2[mt][nt][2] * s.w3[c0];
-            p1 = p1 + h2[mt][nt][3] * s.w3[c0 + 1];
-        }
-        p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, 1);
-        p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, 2);
-        p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, 1);
-        p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, 2);
-        if (t == 0) {
-            sw.y[mt * 16 + g] = p0 + s.b3;
-            sw.y[mt * 16 + g + 8] = p1 + s.b3;
-        }
+        float h2[8][4];
+        mlp_forward_tile(s, sw, mt, h2, true);
     }
     __syncwarp();
 }
