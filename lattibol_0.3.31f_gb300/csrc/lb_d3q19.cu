@@ -128,6 +128,148 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a)
 }
 
 // ---------------------------------------------------------------------------
+// Single-pass Shan-Chen step.  A block owns a SC_TX x SC_TY column tile and
+// marches through a chunk of SC_ZC planes.  For every plane it pulls the
+// populations of its 256 nodes and of the 84-node ring around them, keeps
+// psi of three consecutive planes (with that halo) in shared memory and the
+// pulled populations of the next plane in registers; a plane is relaxed once
+// psi of the plane above is known.  Each population is read from DRAM once
+// per step (the halo pulls are L2 hits) and psi never leaves the SM.  The
+// arithmetic is the two-pass path's (same pulls, rho sum, stencil order), so
+// both produce the same bits.
+// ---------------------------------------------------------------------------
+constexpr int SC_TX = 32, SC_TY = 8, SC_HX = SC_TX + 2, SC_HY = SC_TY + 2;
+constexpr int SC_THREADS = SC_TX * SC_TY;            // 256
+constexpr int SC_HALO = SC_HX * SC_HY - SC_THREADS;  // 84
+
+template <typename S>
+__device__ __forceinline__ float sc_psi_of_node(const D3Args &a, int x, int y, int zz) {
+    const int o = x + a.W * (y + a.H * zz);
+    const uint8_t fl = a.flags[o];
+    if (fl & CELL_WALL) return 0.f;
+    const Nbr3 n(x, y, zz, a.W, a.H, a.D);
+    float g[19];
+    pull_native<S>(a, o, n, fl, g);
+    const float rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8] + g[9] +
+                      g[10] + g[11] + g[12] + g[13] + g[14] + g[15] + g[16] + g[17] + g[18];
+    return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+}
+
+template <typename S, bool MOM>
+__global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args a, int zc) {
+    __shared__ float sp[3][SC_HY][SC_HX];
+    const int tid = threadIdx.x, tx = tid % SC_TX, ty = tid / SC_TX;
+    const int x0 = blockIdx.x * SC_TX, y0 = blockIdx.y * SC_TY, z0 = blockIdx.z * zc;
+    const int x = x0 + tx, y = y0 + ty;
+    // the halo node this thread also handles (tid < 84): two rows of 34, then
+    // the two side columns of 8
+    int hx = 0, hy = 0;
+    if (tid < 2 * SC_HX) {
+        hx = tid % SC_HX - 1;
+        hy = tid < SC_HX ? -1 : SC_TY;
+    } else if (tid < SC_HALO) {
+        hx = (tid - 2 * SC_HX) < SC_TY ? -1 : SC_TX;
+        hy = (tid - 2 * SC_HX) % SC_TY;
+    }
+    const int hxg = (x0 + hx + a.W) % a.W, hyg = (y0 + hy + a.H) % a.H;
+
+    float g_cur[19], g_next[19];
+    uint8_t fl_cur = 0, fl_next = 0;
+    // psi (and, for the own node, the populations) of plane zl into ring slot s
+    auto load_plane = [&](int zl, int s, bool keep) {
+        const int zz = (zl % a.D + a.D) % a.D;
+        const int o = x + a.W * (y + a.H * zz);
+        const uint8_t fl = a.flags[o];
+        float psi = 0.f;
+        if (!(fl & CELL_WALL)) {
+            const Nbr3 n(x, y, zz, a.W, a.H, a.D);
+            pull_native<S>(a, o, n, fl, g_next);
+            const float rho = g_next[0] + g_next[1] + g_next[2] + g_next[3] + g_next[4] +
+                              g_next[5] + g_next[6] + g_next[7] + g_next[8] + g_next[9] +
+                              g_next[10] + g_next[11] + g_next[12] + g_next[13] + g_next[14] +
+                              g_next[15] + g_next[16] + g_next[17] + g_next[18];
+            psi = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+        }
+        if (keep) fl_next = fl;
+        sp[s][ty + 1][tx + 1] = psi;
+        if (tid < SC_HALO) sp[s][hy + 1][hx + 1] = sc_psi_of_node<S>(a, hxg, hyg, zz);
+    };
+
+    load_plane(z0 - 1, 0, false);
+    load_plane(z0, 1, true);
+#pragma unroll
+    for (int k = 0; k < 19; k++) g_cur[k] = g_next[k];
+    fl_cur = fl_next;
+    for (int z = z0; z < z0 + zc; z++) {
+        const int r = z - z0 + 1;  // ring index of plane z
+        __syncthreads();           // slot (r+1)%3 held plane z-2, read by the last iteration
+        load_plane(z + 1, (r + 1) % 3, true);
+        __syncthreads();
+        if (!(fl_cur & CELL_WALL)) {
+            const int o = x + a.W * (y + a.H * z);
+            float rho, ux, uy, uz;
+            d3q19_moments(g_cur, rho, ux, uy, uz);
+            if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+            float ex = ux, ey = uy, ez = uz;
+            if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
+            if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
+            if (a.Fz != 0.f) ez = uz + a.Fz / (rho * a.tau_inv);
+            float IFx = 0.f, IFy = 0.f, IFz = 0.f;
+#pragma unroll
+            for (int k = 1; k < 19; k++) {
+                const int s = (r + d3_cz(k) + 3) % 3;
+                const float t = (k < 7 ? a.w1 : a.w7) *
+                                sp[s][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
+                if (d3_cx(k) > 0) IFx = IFx + t; else if (d3_cx(k) < 0) IFx = IFx - t;
+                if (d3_cy(k) > 0) IFy = IFy + t; else if (d3_cy(k) < 0) IFy = IFy - t;
+                if (d3_cz(k) > 0) IFz = IFz + t; else if (d3_cz(k) < 0) IFz = IFz - t;
+            }
+            const float gp = -a.G * sp[r % 3][ty + 1][tx + 1];
+            ex = ex + (gp * IFx) / (a.tau_inv * rho);
+            ey = ey + (gp * IFy) / (a.tau_inv * rho);
+            ez = ez + (gp * IFz) / (a.tau_inv * rho);
+            d3q19_bgk(g_cur, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+            S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
+#pragma unroll
+            for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g_cur[k], a.wr[k]);
+        } else if (MOM) {
+            const int o = x + a.W * (y + a.H * z);
+            a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < 19; k++) g_cur[k] = g_next[k];
+        fl_cur = fl_next;
+    }
+}
+
+// z-chunk of the marching kernel for a lattice, 0 if the shape does not tile
+int sc_march_chunk(int W, int H, int D) {
+    if (W % SC_TX || H % SC_TY) return 0;
+    for (int zc : {32, 16, 8})
+        if (D % zc == 0) return zc;
+    return 0;
+}
+
+template <typename S>
+static cudaError_t sc_march_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
+    const dim3 g(a.W / SC_TX, a.H / SC_TY, a.D / zc);
+    if (mom) d3q19_sc_march_kernel<S, true><<<g, SC_THREADS, 0, s>>>(a, zc);
+    else d3q19_sc_march_kernel<S, false><<<g, SC_THREADS, 0, s>>>(a, zc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaStream_t s) {
+    const int zc = sc_march_chunk(a.W, a.H, a.D);
+    if (!zc) return cudaErrorInvalidValue;
+    switch (storage) {
+    case 0: return sc_march_launch<float>(a, mom, zc, s);
+    case 1: return sc_march_launch<__half>(a, mom, zc, s);
+    case 2: return sc_march_launch<__nv_bfloat16>(a, mom, zc, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
 // Reference-exact standalone streaming, src/streaming.cu:84-163: in-place
 // swap of f_k(o) and f_opp(k)(o + c_k) for the nine owned slots.  Every
 // (node, slot) belongs to exactly one pair and each pair to exactly one

@@ -50,6 +50,10 @@ cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, c
 // native mode with storage kind (0 f32, 1 f16, 2 bf16) and optional Shan-Chen
 // (sc: the density pass writing a.psi, then the fused step reading it)
 cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc, cudaStream_t s);
+// single-pass Shan-Chen step (psi halo in shared memory, z-marching tiles);
+// usable when sc_march_chunk(W, H, D) != 0
+int sc_march_chunk(int W, int H, int D);
+cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaStream_t s);
 // equilibrium written in 16-bit deviation storage (storage 1 or 2; Pop holds
 // the storage arrays reinterpreted as float*)
 cudaError_t launch_d3q19_equilibrium_storage(const Pop<19> &p, const float *rho, const float *ux,

@@ -3,8 +3,9 @@
 * FP16 / BF16 storage without Shan-Chen is bit-exact against the oracle with
   the storage emulated (each value kept as w_k*rho_ref + widen(narrow(f -
   w_k*rho_ref)), computed in float exactly like the kernel's load/store).
-* Shan-Chen uses psi = 1 - exp(-rho); CUDA's expf and libm may differ by an
-  ulp, so those cases carry tolerances, stated per test.
+* Shan-Chen (psi = 1 - exp(-rho), exp evaluated by the library's own float
+  function on both sides) is bit-exact too, through both the single-pass
+  z-marching kernel and the separate psi pass.
 * The spinodal error study reports rho L2 error and mass drift of the FP32,
   FP16 and BF16 storage forms against the FP64 oracle (printed; bounds
   asserted).
@@ -189,3 +190,48 @@ def test_spinodal_error_vs_fp64(pkg, oracle):
         name, h = key.split("@")
         assert v["err"] < ({"f32": 1e-3}.get(name, 0.2) if h == "50" else 1.0), (key, v)
         assert v["mass_drift"] < {"f32": 5e-5, "f16": 1e-3, "bf16": 1e-2}[name], (key, v)
+
+
+@pytest.mark.parametrize("tuning", [0x100, 0x102], ids=["single_pass", "two_pass"])
+@pytest.mark.parametrize("storage", [0, 2], ids=["f32", "bf16"])
+def test_shan_chen_paths_with_walls_vs_oracle(pkg, oracle, tuning, storage):
+    """Both Shan-Chen paths (single-pass z-marching with the psi halo in
+    shared memory, and the separate psi pass) on a 64x16x64 box with walls,
+    a moving lid and a body force, over several z chunks: bit-exact against
+    the oracle."""
+    W, H, D = 64, 16, 64
+    N = W * H * D
+    fl = np.zeros((D, H, W), np.uint8)
+    fl[0, :, :] = 1
+    fl[-1, :, :] = 3
+    z, y, x = np.mgrid[0:D, 0:H, 0:W]
+    fl[(x - 20) ** 2 + (y - 8) ** 2 + (z - 30) ** 2 <= 9] = 1
+    flags = fl.reshape(-1)
+    rng = np.random.default_rng(17)
+    rho = (0.693 * (1 + 0.01 * rng.uniform(-1, 1, N))).astype(np.float32)
+    zero = np.zeros(N, np.float32)
+    F = (np.float32(2e-6), np.float32(0), np.float32(1e-6))
+    lat = pkg.Lattice(19, W, H, D, tau_inv=1.0, G=-5.0, psi_form=pkg.abi.LB_PSI_EXP1,
+                      force=F, wall_u=(0.02, 0, 0), storage=storage, rho_ref=0.693,
+                      tuning=tuning, graph_steps=4)
+    lat.set_flags(flags)
+    f = oracle.d3q19_equilibrium(rho, zero, zero, zero, *pkg.W3)
+    lat.set_populations(f)
+    wr = oracle.storage_offsets(19, 0.693)
+    if storage:
+        oracle.quantize_dev(f, wr, flags, storage)
+    lat.step(12)
+    corr = oracle.wall_correction(19, (0.02, 0, 0))
+    mom = [np.zeros(N, np.float32) for _ in range(4)]
+    psi = np.zeros(N, np.float32)
+    for _ in range(12):
+        oracle.d3q19_stream_native(f, flags, corr, W, H, D)
+        oracle.d3q19_collide_native(f, flags, mom, W, H, D, *pkg.W3, np.float32(1.0), F,
+                                    G=-5.0, psi=psi, psi_form=oracle.PSI_EXP1)
+        if storage:
+            oracle.quantize_dev(f, wr, flags, storage)
+    fluid = (flags & 1) == 0
+    assert beq(lat.populations()[:, fluid], f[:, fluid])
+    rho_g, ux_g, uy_g, uz_g = lat.moments()
+    assert beq(rho_g, mom[3]) and beq(uz_g, mom[2])
+    lat.close()
