@@ -24,6 +24,7 @@ struct lb_ctx {
     uint8_t *sb = nullptr;               // reference mode: solid_bound
     float *mom = nullptr;                // rho, ux, uy, uz (each `stride` floats)
     float *sc = nullptr;                 // psi (D3Q19, D2Q9) and ueq_x, ueq_y (D2Q9)
+    float *stage = nullptr;              // 16-bit storage: one float array for conversions
     double *red = nullptr;               // reduction partials + result
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
@@ -285,6 +286,7 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sb, c->stride);
     if (e == cudaSuccess) e = cudaMalloc(&c->mom, sizeof(float) * c->stride * 4);
     if (e == cudaSuccess && nsc) e = cudaMalloc(&c->sc, sizeof(float) * c->stride * nsc);
+    if (e == cudaSuccess && c->esize != 4) e = cudaMalloc(&c->stage, sizeof(float) * c->stride);
     // reduction partials, 7 results, then 4 floats (2 doubles) for lb_probe
     if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 16));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -315,6 +317,7 @@ int lb_destroy(lb_ctx *c) {
     if (c->sb) cudaFree(c->sb);
     if (c->mom) cudaFree(c->mom);
     if (c->sc) cudaFree(c->sc);
+    if (c->stage) cudaFree(c->stage);
     if (c->red) cudaFree(c->red);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -337,7 +340,7 @@ int lb_set_flags(lb_ctx *c, const uint8_t *flags) {
 }
 
 // populations cross the API as float; 16-bit storage converts on the device
-// through the first moment field as a staging array
+// through a staging array of its own (the moment fields stay untouched)
 int lb_set_populations(lb_ctx *c, const float *f) {
     if (!c || !f) return fail(c, LB_ERR_ARG, "lb_set_populations: null argument");
     for (int k = 0; k < c->Q; k++) {
@@ -347,10 +350,10 @@ int lb_set_populations(lb_ctx *c, const float *f) {
                                    cudaMemcpyHostToDevice, c->stream));
         } else {
             LB_TRY(c, "lb_set_populations",
-                   cudaMemcpyAsync(mom_k(c, 0), f + (long)k * c->N, sizeof(float) * c->N,
+                   cudaMemcpyAsync(c->stage, f + (long)k * c->N, sizeof(float) * c->N,
                                    cudaMemcpyHostToDevice, c->stream));
             LB_TRY(c, "lb_set_populations",
-                   launch_to_storage(mom_k(c, 0), pop_k(c, c->cur, k), c->N, c->wr[k],
+                   launch_to_storage(c->stage, pop_k(c, c->cur, k), c->N, c->wr[k],
                                      c->cfg.storage, c->stream));
             c->launches += 1;
         }
@@ -365,10 +368,10 @@ int lb_get_populations(lb_ctx *c, float *f) {
         const float *src = pop_k(c, c->cur, k);
         if (c->esize != 4) {
             LB_TRY(c, "lb_get_populations",
-                   launch_from_storage(pop_k(c, c->cur, k), mom_k(c, 3), c->N, c->wr[k],
+                   launch_from_storage(pop_k(c, c->cur, k), c->stage, c->N, c->wr[k],
                                        c->cfg.storage, c->stream));
             c->launches += 1;
-            src = mom_k(c, 3);
+            src = c->stage;
         }
         LB_TRY(c, "lb_get_populations",
                cudaMemcpyAsync(f + (long)k * c->N, src, sizeof(float) * c->N,
