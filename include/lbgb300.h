@@ -162,8 +162,10 @@ typedef enum {
 /* launch tuning (lb_config.tuning); results do not depend on it */
 #define LB_TUNE_DEFAULT 0      /* the library's measured choice */
 #define LB_TUNE_EXPLICIT 0x100 /* use exactly the bits below */
-#define LB_TUNE_SC_TWO_PASS 0x002 /* D3Q19 Shan-Chen: separate psi pass instead of the
-                                     single-pass z-marching kernel (same results) */
+#define LB_TUNE_SC_SINGLE_PASS 0x002 /* D3Q19 Shan-Chen: the single-pass z-marching
+                                        kernel (psi halo in shared memory) instead of
+                                        the separate psi pass; same results, measured
+                                        slower (17.7 vs 25.9 GLUPS at 256^3) */
 #define LB_TUNE_REVERSE 0x001  /* sweep the lattice in the opposite order on every
                                   other step, so a step starts where the previous
                                   one ended and its last writes are still in L2 */
