@@ -136,6 +136,8 @@ typedef enum {
     LB_ERR_STATE = -3,   /* call not valid in the context's current state */
     LB_ERR_NOMEM = -4,   /* device allocation failed */
     LB_ERR_DEVICE = -5,  /* a kernel reported a device-side error (NaN census, bounds) */
+    LB_ERR_IO = -6,      /* a file could not be opened, read or written, or its format
+                            is not supported */
 } lb_status;
 
 #define LB_D2Q9 9
@@ -301,6 +303,94 @@ int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_
  * its extents */
 int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **uz);
 int lb_extents(const lb_ctx *ctx, int *nx, int *ny, int *nz);
+
+/* ======================================================================== */
+/* Part 5: case files -- the reference's Input class (src/input.cpp) and    */
+/* the initial state its Simulation constructors build                      */
+/* ======================================================================== */
+
+/* Functions without a context report failures through lb_abi_last_error(). */
+
+/* the parameter file (.dat), one value per line, read as reference
+ * src/input.cpp:51-94 (Input::loadParameters) reads it: a missing line or one
+ * that is not a number reads as 0; lines after the 13th are ignored */
+typedef struct {
+    int device_count;   /* line 1 */
+    int max_dim;        /* line 2; <= 1 means a 2-D case (stored as 1) */
+    float ux, uy, uz;   /* lines 3-5: inlet and initial velocity */
+    float rho;          /* line 6: outlet and initial density */
+    float viscosity;    /* line 7 */
+    int update_steps;   /* line 8: steps between two display updates */
+    float ext_f[3];     /* lines 9-11: body force (Fx, Fy, Fz) */
+    float G;            /* line 12: Shan-Chen interaction strength */
+    float G_ads;        /* line 13: fluid-solid adhesion strength */
+    float tau_inv;      /* 1 / (3 viscosity + 0.5), src/input.cpp:168-171 */
+    float min_u, max_u, min_rho, max_rho; /* colour scales, src/input.cpp:88-91 */
+} lb_case_params;
+
+/* reference src/input.cpp:51-94; LB_ERR_IO when the file cannot be opened */
+int lb_case_load_parameters(const char *path, lb_case_params *out);
+
+/* The solid mask of a 2-D case from a Windows bitmap, as reference
+ * src/input.cpp:96-116 (Input::loadSolids): a node is solid where the pixel
+ * is opaque black, solids[x + y*width] with y = 0 the top row of the image.
+ * Supported: uncompressed 1/4/8/16/24/32 bits per pixel and BI_BITFIELDS
+ * 16/32, bottom-up or top-down.  Call with solids = NULL to read the size;
+ * capacity is the size of solids in bytes. */
+int lb_case_load_solids_bmp(const char *path, int *width, int *height, uint8_t *solids,
+                            size_t capacity);
+
+/* The initial D2Q9 state of reference src/simulation_d2q9.cu:100-334 for one
+ * device over the whole width, in host memory: f is 9 arrays of
+ * width*height floats (f[k*N + node]), the other outputs N values each
+ * (psi, ueq_x, ueq_y may be NULL).  Values the reference leaves unset
+ * (solid nodes of a Shan-Chen case) are 0, as fresh pages of the reference's
+ * allocations are. */
+int lb_case_init_d2q9(const lb_case_params *p, int width, int height, const uint8_t *solids,
+                      float *f, float *ux, float *uy, float *rho, float *psi, float *ueq_x,
+                      float *ueq_y, uint8_t *solid_bound);
+
+/* The initial D3Q19 state of reference src/simulation_d3q19.cu:99-204 (one
+ * device): uniform equilibrium at (ux, uy, uz, rho) and the solid_bound rule.
+ * Like the reference it sets uz only at node 0 (uz[i > 0] = 0). */
+int lb_case_init_d3q19(const lb_case_params *p, int width, int height, int depth,
+                       const uint8_t *solids, float *f, float *ux, float *uy, float *uz,
+                       float *rho, uint8_t *solid_bound);
+
+/* ======================================================================== */
+/* Part 6: output files and checkpoints                                     */
+/* ======================================================================== */
+
+/* The VTK image file "<dir>/rIIIIpDD.vti" of reference src/output.cpp:96-155
+ * (Output::saveVTK): ASCII, "Pressure" = rho, "Velocity" = (ux, uy, uz) in
+ * 3-D and (ux, -uy, 0) in 2-D (length == 1), x extent width+1 points with
+ * a 0 closing every row.  vtk_id 0..9999, device_id 0..99; uz may be NULL in
+ * 2-D. */
+int lb_vtk_save(const char *dir, int vtk_id, int device_id, int width, int height, int length,
+                const float *rho, const float *ux, const float *uy, const float *uz);
+/* the parallel index "<dir>/rIIII.pvti" of reference src/output.cpp:52-94
+ * (Output::saveParVTK) naming device_count pieces of width nodes each */
+int lb_vtk_save_parallel(const char *dir, int vtk_id, int device_count, int width, int height,
+                         int length);
+/* the moments of a context's last step as a VTK file (device 0 of 1) */
+int lb_vtk_save_ctx(lb_ctx *ctx, const char *dir, int vtk_id);
+
+/* Checkpoints of a context: configuration, step count, cell flags, the
+ * populations in their stored type (16-bit storage is saved as stored, so a
+ * resumed run is bit-identical to an uninterrupted one) and the moment
+ * fields, each section with a CRC-32.  The file is written beside the target
+ * and renamed over it when complete. */
+int lb_checkpoint_save(lb_ctx *ctx, const char *path);
+/* restore into a context created with the same lattice, extents, mode and
+ * storage (LB_ERR_ARG otherwise; LB_ERR_IO for a damaged file) */
+int lb_checkpoint_load(lb_ctx *ctx, const char *path);
+/* a new context with the checkpoint's configuration and state */
+int lb_checkpoint_create(const char *path, lb_ctx **out);
+/* the configuration and step count stored in a checkpoint */
+int lb_checkpoint_info(const char *path, lb_config *cfg, int64_t *steps);
+/* time steps a context has advanced since lb_create (restored by
+ * lb_checkpoint_load) */
+int64_t lb_steps_done(const lb_ctx *ctx);
 
 /* ---- device helpers (tests and hosts without their own allocator) ------ */
 int lb_device_count(int *n);

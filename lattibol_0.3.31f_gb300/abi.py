@@ -73,8 +73,20 @@ class lb_run_params_d3q19(ctypes.Structure):
                                               "uz_in", "rho_out")] + [("cursor", ctypes.c_int * 3)]
 
 
+class lb_case_params(ctypes.Structure):
+    """The parameter file of a case (reference src/input.cpp:51-94)."""
+    _fields_ = [("device_count", ctypes.c_int), ("max_dim", ctypes.c_int),
+                ("ux", ctypes.c_float), ("uy", ctypes.c_float), ("uz", ctypes.c_float),
+                ("rho", ctypes.c_float), ("viscosity", ctypes.c_float),
+                ("update_steps", ctypes.c_int), ("ext_f", ctypes.c_float * 3),
+                ("G", ctypes.c_float), ("G_ads", ctypes.c_float), ("tau_inv", ctypes.c_float),
+                ("min_u", ctypes.c_float), ("max_u", ctypes.c_float),
+                ("min_rho", ctypes.c_float), ("max_rho", ctypes.c_float)]
+
+
 # constants of lbgb300.h
 LB_OK, LB_ERR_ARG, LB_ERR_CUDA, LB_ERR_STATE, LB_ERR_NOMEM, LB_ERR_DEVICE = 0, -1, -2, -3, -4, -5
+LB_ERR_IO = -6
 LB_D2Q9, LB_D3Q19 = 9, 19
 LB_MODE_REFERENCE, LB_MODE_NATIVE = 0, 1
 LB_STORE_F32, LB_STORE_F16, LB_STORE_BF16 = 0, 1, 2
@@ -164,6 +176,22 @@ PROTOTYPES = [
                                      _c.c_void_p, _c.c_void_p, _c.POINTER(_c.c_double)]),
     ("lb_device_fields", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_void_p)] * 4),
     ("lb_extents", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3),
+    ("lb_case_load_parameters", _c.c_int, [_c.c_char_p, _c.POINTER(lb_case_params)]),
+    ("lb_case_load_solids_bmp", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_int),
+                                           _c.POINTER(_c.c_int), _c.c_void_p, _c.c_size_t]),
+    ("lb_case_init_d2q9", _c.c_int, [_c.POINTER(lb_case_params), _c.c_int, _c.c_int]
+     + [_c.c_void_p] * 9),
+    ("lb_case_init_d3q19", _c.c_int, [_c.POINTER(lb_case_params), _c.c_int, _c.c_int, _c.c_int]
+     + [_c.c_void_p] * 7),
+    ("lb_vtk_save", _c.c_int, [_c.c_char_p] + [_c.c_int] * 5 + [_c.c_void_p] * 4),
+    ("lb_vtk_save_parallel", _c.c_int, [_c.c_char_p] + [_c.c_int] * 5),
+    ("lb_vtk_save_ctx", _c.c_int, [_c.c_void_p, _c.c_char_p, _c.c_int]),
+    ("lb_checkpoint_save", _c.c_int, [_c.c_void_p, _c.c_char_p]),
+    ("lb_checkpoint_load", _c.c_int, [_c.c_void_p, _c.c_char_p]),
+    ("lb_checkpoint_create", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_void_p)]),
+    ("lb_checkpoint_info", _c.c_int, [_c.c_char_p, _c.POINTER(lb_config),
+                                      _c.POINTER(_c.c_int64)]),
+    ("lb_steps_done", _c.c_int64, [_c.c_void_p]),
     ("lb_device_count", _c.c_int, [_c.POINTER(_c.c_int)]),
     ("lb_malloc", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
     ("lb_free", _c.c_int, [_c.c_void_p]),

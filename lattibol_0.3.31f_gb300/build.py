@@ -20,7 +20,7 @@ LIB = os.path.join(LIB_DIR, "liblbgb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(ROOT, "include")]
+                     "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 
 def _nvcc():

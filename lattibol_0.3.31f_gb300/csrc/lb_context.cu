@@ -3,6 +3,9 @@
 // the fused kernel ping-pongs between (FP32, or 16-bit deviations from
 // w_k*rho_ref), batches of steps replayed from captured CUDA graphs, FP64
 // reductions; plus the drop-in reductions and the small device helpers.
+#include <algorithm>
+#include <cstddef>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -36,6 +39,7 @@ struct lb_ctx {
     ClosureArgs closure{};
     bool flags_set = false;
     int64_t launches = 0;
+    int64_t steps = 0;                   // time steps since lb_create (or the checkpoint's)
     std::string err;
 };
 
@@ -435,6 +439,7 @@ int lb_step(lb_ctx *c, int nsteps) {
     }
     LB_TRY(c, "lb_step", step_once(c, c->cur, true));
     c->cur = 1 - c->cur;
+    c->steps += nsteps;
     return LB_OK;
 }
 
@@ -485,6 +490,7 @@ int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
     for (int i = 0; i < nsteps; i++) {
         LB_TRY(c, "lb_run_probe", step_once(c, c->cur, true));
         c->cur = 1 - c->cur;
+        c->steps += 1;
         const int rc = lb_probe(c, x, y, z, value);
         if (rc != LB_OK) return rc;
     }
@@ -530,6 +536,274 @@ int64_t lb_launch_count(const lb_ctx *c) { return c ? c->launches : -1; }
 int lb_wall_correction(const lb_ctx *c, float *corr) {
     if (!c || !corr) return LB_ERR_ARG;
     memcpy(corr, c->corr, sizeof(float) * c->Q);
+    return LB_OK;
+}
+
+int64_t lb_steps_done(const lb_ctx *c) { return c ? c->steps : -1; }
+
+}  // extern "C"
+
+// ----------------------------------------------------------------- checkpoints
+//
+// File layout (the host's byte order, marked in the header):
+//   256-byte header (CkptHeader), then three sections:
+//   flags        N bytes, the context's cell flags
+//   populations  Q arrays of N values in the stored type (4 or 2 bytes)
+//   moments      rho, ux, uy (, uz for D3Q19): N floats each
+// Each section and the header carry a CRC-32 (reflected, polynomial
+// 0xEDB88320).  A load checks every CRC before it changes the context.
+namespace {
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, header_bytes, byte_order;
+    int32_t lattice, nx, ny, nz, mode, storage, psi_form, graph_steps, tuning;
+    float tau_inv, force[3], u_in[3], rho_out, wall_u[3], G, G_ads, rho_ref;
+    int64_t steps;
+    uint64_t flag_bytes, pop_bytes, mom_bytes;
+    uint32_t crc_flags, crc_pop, crc_mom, crc_header;
+    uint8_t pad[96];
+};
+static_assert(sizeof(CkptHeader) == 256, "checkpoint header is 256 bytes");
+constexpr char CKPT_MAGIC[8] = {'L', 'B', 'G', 'B', 'C', 'K', 'P', 'T'};
+constexpr uint32_t CKPT_BYTE_ORDER = 0x01020304u;
+
+uint32_t crc32_update(uint32_t crc, const void *data, size_t n) {
+    static uint32_t table[256];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t r = i;
+            for (int j = 0; j < 8; j++) r = (r & 1) ? (r >> 1) ^ 0xEDB88320u : r >> 1;
+            table[i] = r;
+        }
+    });
+    const uint8_t *p = static_cast<const uint8_t *>(data);
+    crc = ~crc;
+    for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+    return ~crc;
+}
+
+int n_moments(const lb_ctx *c) { return c->Q == 19 ? 4 : 3; }
+
+void header_from_config(const lb_config &g, CkptHeader &h) {
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, CKPT_MAGIC, 8);
+    h.version = 1;
+    h.header_bytes = sizeof(CkptHeader);
+    h.byte_order = CKPT_BYTE_ORDER;
+    h.lattice = g.lattice; h.nx = g.nx; h.ny = g.ny; h.nz = g.nz;
+    h.mode = g.mode; h.storage = g.storage; h.psi_form = g.psi_form;
+    h.graph_steps = g.graph_steps; h.tuning = g.tuning;
+    h.tau_inv = g.tau_inv; h.rho_out = g.rho_out; h.G = g.G; h.G_ads = g.G_ads;
+    h.rho_ref = g.rho_ref;
+    for (int i = 0; i < 3; i++) {
+        h.force[i] = g.force[i]; h.u_in[i] = g.u_in[i]; h.wall_u[i] = g.wall_u[i];
+    }
+}
+
+void config_from_header(const CkptHeader &h, lb_config &g) {
+    lb_config_default(&g, h.lattice, h.nx, h.ny, h.nz);
+    g.mode = h.mode; g.storage = h.storage; g.psi_form = h.psi_form;
+    g.graph_steps = h.graph_steps; g.tuning = h.tuning;
+    g.tau_inv = h.tau_inv; g.rho_out = h.rho_out; g.G = h.G; g.G_ads = h.G_ads;
+    g.rho_ref = h.rho_ref;
+    for (int i = 0; i < 3; i++) {
+        g.force[i] = h.force[i]; g.u_in[i] = h.u_in[i]; g.wall_u[i] = h.wall_u[i];
+    }
+}
+
+// the header, checked for magic, version, byte order and its own CRC
+std::string read_header(FILE *fp, CkptHeader &h) {
+    if (fread(&h, sizeof h, 1, fp) != 1) return "not a checkpoint (short header)";
+    if (memcmp(h.magic, CKPT_MAGIC, 8) != 0) return "not a checkpoint (magic)";
+    if (h.byte_order != CKPT_BYTE_ORDER) return "checkpoint written with another byte order";
+    if (h.version != 1 || h.header_bytes != sizeof(CkptHeader))
+        return "unsupported checkpoint version";
+    const uint32_t crc = crc32_update(0, &h, offsetof(CkptHeader, crc_header));
+    if (crc != h.crc_header) return "checkpoint header damaged (CRC)";
+    if ((h.lattice != LB_D2Q9 && h.lattice != LB_D3Q19) || h.nx < 1 || h.ny < 1 || h.nz < 1)
+        return "checkpoint header has bad extents";
+    return "";
+}
+
+// streams `bytes` bytes of the file through f(chunk, n) in pieces of at most
+// `piece` bytes; false on a short read
+template <class F>
+bool stream_section(FILE *fp, uint64_t bytes, std::vector<uint8_t> &buf, F &&f) {
+    while (bytes > 0) {
+        const size_t n = (size_t)std::min<uint64_t>(bytes, buf.size());
+        if (fread(buf.data(), 1, n, fp) != n) return false;
+        f(buf.data(), n);
+        bytes -= n;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lb_checkpoint_save(lb_ctx *c, const char *path) {
+    if (!c || !path) return fail(c, LB_ERR_ARG, "lb_checkpoint_save: null argument");
+    const long N = c->N;
+    const size_t pop_k_bytes = (size_t)N * c->esize;
+    CkptHeader h;
+    header_from_config(c->cfg, h);
+    h.steps = c->steps;
+    h.flag_bytes = (uint64_t)N;
+    h.pop_bytes = (uint64_t)pop_k_bytes * c->Q;
+    h.mom_bytes = (uint64_t)N * sizeof(float) * n_moments(c);
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *fp = fopen(tmp.c_str(), "wb");
+    if (!fp) return fail(c, LB_ERR_IO, "lb_checkpoint_save: cannot create " + tmp);
+    auto bail = [&](int code, const std::string &msg) {
+        fclose(fp);
+        remove(tmp.c_str());
+        return fail(c, code, "lb_checkpoint_save: " + msg);
+    };
+    // the header goes first as a placeholder and is rewritten with the CRCs
+    if (fwrite(&h, sizeof h, 1, fp) != 1) return bail(LB_ERR_IO, "write failed");
+    std::vector<uint8_t> buf(std::max<size_t>(pop_k_bytes, (size_t)N * sizeof(float)));
+    auto section = [&](const void *dev, size_t bytes, uint32_t &crc) -> int {
+        cudaError_t e = cudaMemcpyAsync(buf.data(), dev, bytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, "lb_checkpoint_save", e);
+        crc = crc32_update(crc, buf.data(), bytes);
+        if (fwrite(buf.data(), 1, bytes, fp) != bytes) return LB_ERR_IO;
+        return LB_OK;
+    };
+    int rc = LB_OK;
+    LB_TRY(c, "lb_checkpoint_save", cudaStreamSynchronize(c->stream));
+    rc = section(c->flags, (size_t)N, h.crc_flags);
+    for (int k = 0; k < c->Q && rc == LB_OK; k++) rc = section(pop_k(c, c->cur, k), pop_k_bytes, h.crc_pop);
+    for (int i = 0; i < n_moments(c) && rc == LB_OK; i++)
+        rc = section(mom_k(c, i), (size_t)N * sizeof(float), h.crc_mom);
+    if (rc == LB_ERR_CUDA) {
+        fclose(fp);
+        remove(tmp.c_str());
+        return rc;
+    }
+    if (rc != LB_OK) return bail(LB_ERR_IO, "write failed");
+    h.crc_header = crc32_update(0, &h, offsetof(CkptHeader, crc_header));
+    if (fseek(fp, 0, SEEK_SET) != 0 || fwrite(&h, sizeof h, 1, fp) != 1)
+        return bail(LB_ERR_IO, "write failed");
+    if (fclose(fp) != 0) {
+        remove(tmp.c_str());
+        return fail(c, LB_ERR_IO, "lb_checkpoint_save: write failed");
+    }
+    if (rename(tmp.c_str(), path) != 0) {
+        remove(tmp.c_str());
+        return fail(c, LB_ERR_IO, std::string("lb_checkpoint_save: cannot rename to ") + path);
+    }
+    return LB_OK;
+}
+
+int lb_checkpoint_info(const char *path, lb_config *cfg, int64_t *steps) {
+    if (!path) return LB_ERR_ARG;
+    FILE *fp = fopen(path, "rb");
+    if (!fp) {
+        abi_record_error("lb_checkpoint_info", (std::string("cannot open ") + path).c_str());
+        return LB_ERR_IO;
+    }
+    CkptHeader h;
+    const std::string why = read_header(fp, h);
+    fclose(fp);
+    if (!why.empty()) {
+        abi_record_error("lb_checkpoint_info", why.c_str());
+        return LB_ERR_IO;
+    }
+    if (cfg) config_from_header(h, *cfg);
+    if (steps) *steps = h.steps;
+    return LB_OK;
+}
+
+int lb_checkpoint_load(lb_ctx *c, const char *path) {
+    if (!c || !path) return fail(c, LB_ERR_ARG, "lb_checkpoint_load: null argument");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(c, LB_ERR_IO, std::string("lb_checkpoint_load: cannot open ") + path);
+    auto bail = [&](int code, const std::string &msg) {
+        fclose(fp);
+        return fail(c, code, "lb_checkpoint_load: " + msg);
+    };
+    CkptHeader h;
+    std::string why = read_header(fp, h);
+    if (!why.empty()) return bail(LB_ERR_IO, why);
+    const lb_config &g = c->cfg;
+    if (h.lattice != g.lattice || h.nx != g.nx || h.ny != g.ny || h.nz != g.nz ||
+        h.mode != g.mode || h.storage != g.storage)
+        return bail(LB_ERR_ARG, "lattice, extents, mode or storage differ from the context's");
+    const long N = c->N;
+    const size_t pop_k_bytes = (size_t)N * c->esize;
+    const size_t mom_k_bytes = (size_t)N * sizeof(float);
+    if (h.flag_bytes != (uint64_t)N || h.pop_bytes != (uint64_t)pop_k_bytes * c->Q ||
+        h.mom_bytes != (uint64_t)mom_k_bytes * n_moments(c))
+        return bail(LB_ERR_IO, "section sizes do not match the header");
+    // pass 1: every CRC, before anything in the context changes
+    std::vector<uint8_t> buf(std::max(pop_k_bytes, mom_k_bytes));
+    uint32_t crc[3] = {0, 0, 0};
+    const uint64_t sizes[3] = {h.flag_bytes, h.pop_bytes, h.mom_bytes};
+    for (int s = 0; s < 3; s++)
+        if (!stream_section(fp, sizes[s], buf, [&](const uint8_t *p, size_t n) {
+                crc[s] = crc32_update(crc[s], p, n);
+            }))
+            return bail(LB_ERR_IO, "file is truncated");
+    if (crc[0] != h.crc_flags || crc[1] != h.crc_pop || crc[2] != h.crc_mom)
+        return bail(LB_ERR_IO, "checkpoint data damaged (CRC)");
+    // pass 2: upload
+    if (fseek(fp, (long)sizeof(CkptHeader), SEEK_SET) != 0) return bail(LB_ERR_IO, "seek failed");
+    std::vector<uint8_t> flags((size_t)N);
+    if (fread(flags.data(), 1, (size_t)N, fp) != (size_t)N) return bail(LB_ERR_IO, "read failed");
+    auto upload = [&](void *dev, size_t bytes) -> int {
+        if (fread(buf.data(), 1, bytes, fp) != bytes) return LB_ERR_IO;
+        cudaError_t e = cudaMemcpyAsync(dev, buf.data(), bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // buf is reused
+        return e == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+    };
+    int rc = LB_OK;
+    for (int k = 0; k < c->Q && rc == LB_OK; k++) rc = upload(pop_k(c, c->cur, k), pop_k_bytes);
+    for (int i = 0; i < n_moments(c) && rc == LB_OK; i++) rc = upload(mom_k(c, i), mom_k_bytes);
+    fclose(fp);
+    if (rc == LB_ERR_IO) return fail(c, rc, "lb_checkpoint_load: read failed");
+    if (rc != LB_OK) return fail(c, rc, "lb_checkpoint_load: copy to the device failed");
+    rc = lb_set_flags(c, flags.data());  // re-derives the wall-neighbour bits and solid_bound
+    if (rc != LB_OK) return rc;
+    c->steps = h.steps;
+    return LB_OK;
+}
+
+int lb_checkpoint_create(const char *path, lb_ctx **out) {
+    if (!path || !out) return LB_ERR_ARG;
+    *out = nullptr;
+    lb_config cfg;
+    int rc = lb_checkpoint_info(path, &cfg, nullptr);
+    if (rc != LB_OK) return rc;
+    lb_ctx *c = nullptr;
+    rc = lb_create(&cfg, &c);
+    if (rc != LB_OK) {
+        abi_record_error("lb_checkpoint_create", "lb_create failed for the stored configuration");
+        return rc;
+    }
+    rc = lb_checkpoint_load(c, path);
+    if (rc != LB_OK) {
+        abi_record_error("lb_checkpoint_create", c->err.c_str());
+        lb_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return LB_OK;
+}
+
+int lb_vtk_save_ctx(lb_ctx *c, const char *dir, int vtk_id) {
+    if (!c) return LB_ERR_ARG;
+    const long N = c->N;
+    std::vector<float> m((size_t)N * 4, 0.f);
+    int rc = lb_get_moments(c, m.data(), m.data() + N, m.data() + 2 * N,
+                            c->Q == 19 ? m.data() + 3 * N : nullptr);
+    if (rc != LB_OK) return rc;
+    rc = lb_vtk_save(dir, vtk_id, 0, c->cfg.nx, c->cfg.ny, c->cfg.nz, m.data(), m.data() + N,
+                     m.data() + 2 * N, c->Q == 19 ? m.data() + 3 * N : nullptr);
+    if (rc != LB_OK) return fail(c, rc, lb_abi_last_error());
     return LB_OK;
 }
 

@@ -8,6 +8,7 @@ src/simulation_d2q9.cu:336-390), so that the drop-in entry points can be
 driven exactly like the reference's runLBM drives them.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -125,6 +126,40 @@ class Lattice:
         c = np.zeros(self.Q, np.float32)
         self._check(_lib().lb_wall_correction(self.h, _ptr(c)), "lb_wall_correction")
         return c
+
+    def steps_done(self):
+        return _lib().lb_steps_done(self.h)
+
+    def save_checkpoint(self, path):
+        self._check(_lib().lb_checkpoint_save(self.h, os.fsencode(path)), "lb_checkpoint_save")
+
+    def load_checkpoint(self, path):
+        """Restore a checkpoint; returns the library status (LB_ERR_ARG for a
+        checkpoint of another lattice, LB_ERR_IO for a damaged file)."""
+        return _lib().lb_checkpoint_load(self.h, os.fsencode(path))
+
+    def save_vtk(self, directory, vtk_id):
+        self._check(_lib().lb_vtk_save_ctx(self.h, os.fsencode(directory), int(vtk_id)),
+                    "lb_vtk_save_ctx")
+
+    @classmethod
+    def from_checkpoint(cls, path):
+        """A new lattice with the configuration and state of a checkpoint."""
+        L = _lib()
+        h = ctypes.c_void_p()
+        rc = L.lb_checkpoint_create(os.fsencode(path), ctypes.byref(h))
+        if rc != abi.LB_OK:
+            raise LBError("lb_checkpoint_create failed (%d): %s"
+                          % (rc, L.lb_abi_last_error().decode()))
+        self = cls.__new__(cls)
+        cfg = abi.lb_config()
+        L.lb_checkpoint_info(os.fsencode(path), ctypes.byref(cfg), None)
+        self.cfg = cfg
+        self.Q = cfg.lattice
+        self.shape = (cfg.nx, cfg.ny, cfg.nz if cfg.lattice == 19 else 1)
+        self.N = cfg.nx * cfg.ny * self.shape[2]
+        self.h = h
+        return self
 
 
 def sc_coexistence(G, n=4000):

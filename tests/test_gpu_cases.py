@@ -1,0 +1,205 @@
+"""GPU: the reference's sample cases run headless through the drop-in entry
+points (Input -> SimulationD2Q9 -> runLBM), bit-exact against the oracle;
+checkpoint/resume bit-identity; VTK output of a context."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import case_oracle as co
+from test_case_files import fixture_mask, fixture_params, fixtures
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 16
+
+
+def beq(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+
+
+def distinct_2d_cases():
+    cases, masks = fixtures()
+    seen, out = set(), []
+    for e in cases:
+        if "width" not in e:
+            continue
+        key = (e["mask"], json.dumps(e["params"], sort_keys=True))
+        if key not in seen:
+            seen.add(key)
+            out.append(e)
+    return out, masks
+
+
+def make_input(pkg, p, mask):
+    inp = pkg.Input()
+    for k, v in p.items():
+        if k == "ext_f":
+            for i in range(3):
+                inp.p.ext_f[i] = float(v[i])
+        else:
+            setattr(inp.p, k, v if isinstance(v, int) else float(v))
+    inp.setSolids(mask)
+    return inp
+
+
+def oracle_run(oracle, pkg, p, mask, steps):
+    """the reference loop (stream, collide) on the oracle from the case's
+    initial state"""
+    H, W = mask.shape
+    init = co.init_d2q9(p, mask)
+    f = init["f"].copy()
+    mom = [init[k].copy() for k in ("ux", "uy", "rho")]
+    sc = [init[k].copy() for k in ("psi", "ueq_x", "ueq_y")]
+    solid = np.ascontiguousarray(mask.reshape(-1), np.uint8)
+    plot = np.zeros(4 * W * H, np.float32)
+    for _ in range(steps):
+        oracle.d2q9_stream(f, init["solid_bound"], W, H)
+        oracle.d2q9_collide(f, solid, mom, sc, W, H, *pkg.W2, p["tau_inv"], p["ux"], p["uy"],
+                            p["rho"], p["ext_f"][0], p["ext_f"][1], p["G"], p["G_ads"],
+                            plot=plot)
+    return f, mom, sc, plot
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["standalone", "fused"])
+def test_sample_cases_vs_oracle(pkg, oracle, mode):
+    """Every distinct 2-D sample case of the reference (its .dat parameters
+    and .bmp solids) for 16 steps of the reference's own loop: populations,
+    moments, Shan-Chen fields and the plot buffer bit-identical."""
+    L = pkg.lib()
+    cases, masks = distinct_2d_cases()
+    assert len(cases) >= 15
+    assert L.lb_abi_set_mode(mode) == 0
+    try:
+        for e in cases:
+            p, mask = fixture_params(e), fixture_mask(e, masks)
+            sim = pkg.SimulationD2Q9(make_input(pkg, p, mask))
+            sim.runLBM(STEPS)
+            assert sim.getSteps() == STEPS
+            f, mom, sc, plot = oracle_run(oracle, pkg, p, mask, STEPS)
+            assert L.lb_abi_release_d2q9(sim.data.ptr()) == 0
+            assert beq(sim.populations(), f), e["name"]
+            for k, a in zip(("ux", "uy", "rho"), mom):
+                assert beq(sim.field(k), a), (e["name"], k)
+            if p["G"] < 0:
+                for k, a in zip(("psi", "ueq_x", "ueq_y"), sc):
+                    assert beq(sim.field(k), a), (e["name"], k)
+            assert beq(sim.data.plot_data(), plot), e["name"]
+            sim.close()
+    finally:
+        L.lb_abi_set_mode(0)
+
+
+def test_sample_case_vtk_output(pkg, tmp_path):
+    """SimulationD2Q9.saveVTK writes the reference's file pair from the
+    device moments."""
+    cases, masks = distinct_2d_cases()
+    e = min(cases, key=lambda c: c["width"] * c["height"])
+    p, mask = fixture_params(e), fixture_mask(e, masks)
+    sim = pkg.SimulationD2Q9(make_input(pkg, p, mask))
+    sim.runLBM(3)
+    sim.saveVTK(str(tmp_path))
+    H, W = mask.shape
+    text = (tmp_path / "r0000p00.vti").read_text()
+    assert text == co.vtk_text(0, W, H, 1, sim.field("rho"), sim.field("ux"), sim.field("uy"))
+    assert (tmp_path / "r0000.pvti").read_text() == co.pvti_text(0, 1, W, H, 1)
+    sim.close()
+
+
+# ----------------------------------------------------------------- checkpoints
+
+def lattice_cases(pkg):
+    a = pkg.abi
+    rng = np.random.default_rng(21)
+    out = []
+    # D3Q19 channel: walls in y, a moving wall, body force
+    W, H, D = 40, 20, 12
+    fl = np.zeros((D, H, W), np.uint8)
+    fl[:, 0, :] = a.LB_CELL_WALL
+    fl[:, H - 1, :] = a.LB_CELL_WALL | a.LB_CELL_MOVING
+    out.append(("d3q19_native_f32", dict(lattice=19, nx=W, ny=H, nz=D, tau_inv=1 / 0.6,
+                                         force=(1e-5, 0, 0), wall_u=(0.05, 0, 0)),
+                fl.reshape(-1), None))
+    # D3Q19 Shan-Chen with bf16 storage
+    n = 24 ** 3
+    rho = (0.693 * (1 + 0.01 * (2 * rng.random(n) - 1))).astype(np.float32)
+    out.append(("d3q19_sc_bf16", dict(lattice=19, nx=24, ny=24, nz=24, tau_inv=1.0, G=-5.0,
+                                      storage=a.LB_STORE_BF16, rho_ref=0.693),
+                np.zeros(n, np.uint8), rho))
+    # D2Q9 in the reference's semantics: Zou-He, solids, Shan-Chen
+    W2, H2 = 48, 32
+    sol = (rng.random((H2, W2)) < 0.08).astype(np.uint8)
+    out.append(("d2q9_reference_sc", dict(lattice=9, nx=W2, ny=H2, mode=a.LB_MODE_REFERENCE,
+                                          tau_inv=1 / (3 * 0.16667 + 0.5), G=-120.0,
+                                          rho_out=200.0, psi_form=a.LB_PSI_REF),
+                sol.reshape(-1), np.full(W2 * H2, 200.0, np.float32)))
+    return out
+
+
+def build(pkg, kw, flags, rho):
+    kw = dict(kw)
+    lat = pkg.Lattice(kw.pop("lattice"), kw.pop("nx"), kw.pop("ny"), kw.pop("nz", 1),
+                      graph_steps=4, **kw)
+    lat.set_flags(flags)
+    lat.init_equilibrium(rho=rho)
+    return lat
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2], ids=["d3q19_native_f32", "d3q19_sc_bf16",
+                                                "d2q9_reference_sc"])
+def test_checkpoint_resume_is_bit_identical(pkg, tmp_path, idx):
+    name, kw, flags, rho = lattice_cases(pkg)[idx]
+    K = 9
+    a = build(pkg, kw, flags, rho)
+    a.step(2 * K)
+    ref_f, ref_m = a.populations(), a.moments()
+    a.close()
+
+    b = build(pkg, kw, flags, rho)
+    b.step(K)
+    path = tmp_path / (name + ".ckpt")
+    b.save_checkpoint(path)
+    mid_f = b.populations()
+    b.close()
+    assert not os.path.exists(str(path) + ".tmp")
+
+    c = pkg.Lattice.from_checkpoint(path)
+    assert c.steps_done() == K
+    assert beq(c.populations(), mid_f)
+    c.step(K)
+    assert c.steps_done() == 2 * K
+    assert beq(c.populations(), ref_f)
+    for x, y in zip(c.moments(), ref_m):
+        if x is not None:
+            assert beq(x, y)
+    c.close()
+
+    # into an existing context of the same lattice; a damaged copy and a
+    # lattice of another size are refused and leave the context as it was
+    d = build(pkg, kw, flags, rho)
+    before = d.populations()
+    bad = tmp_path / "damaged.ckpt"
+    raw = bytearray(path.read_bytes())
+    raw[256 + d.N + 7] ^= 0x10
+    bad.write_bytes(bytes(raw))
+    assert d.load_checkpoint(bad) == pkg.abi.LB_ERR_IO
+    assert beq(d.populations(), before)
+    assert d.load_checkpoint(path) == pkg.abi.LB_OK
+    assert beq(d.populations(), mid_f) and d.steps_done() == K
+    d.close()
+    kw2 = dict(kw, nx=kw["nx"] + 1)
+    e = pkg.Lattice(kw2.pop("lattice"), kw2.pop("nx"), kw2.pop("ny"), kw2.pop("nz", 1), **kw2)
+    assert e.load_checkpoint(path) == pkg.abi.LB_ERR_ARG
+    e.close()
+
+
+def test_context_vtk_matches_oracle(pkg, tmp_path):
+    name, kw, flags, rho = lattice_cases(pkg)[0]
+    lat = build(pkg, kw, flags, rho)
+    lat.step(5)
+    lat.save_vtk(str(tmp_path), 7)
+    r, ux, uy, uz = lat.moments()
+    text = (tmp_path / "r0007p00.vti").read_text()
+    assert text == co.vtk_text(0, kw["nx"], kw["ny"], kw["nz"], r, ux, uy, uz)
+    lat.close()
