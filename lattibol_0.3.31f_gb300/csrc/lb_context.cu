@@ -95,6 +95,15 @@ float *pop_k(lb_ctx *c, int set, int k) {
 }
 float *mom_k(lb_ctx *c, int i) { return c->mom + (long)i * c->stride; }
 
+// copies the current population set into the other one.  Native-mode wall
+// nodes are never written by a step, so after the caller sets populations
+// both sets must hold them: a wall node then reads the same at every step.
+cudaError_t mirror_sets(lb_ctx *c) {
+    return cudaMemcpyAsync(c->pop[1 - c->cur], c->pop[c->cur],
+                           (size_t)c->esize * c->stride * c->Q, cudaMemcpyDeviceToDevice,
+                           c->stream);
+}
+
 bool sc_on(const lb_ctx *c) {
     return c->cfg.mode == LB_MODE_REFERENCE ? (c->Q == 9 && c->cfg.G < 0.f) : c->cfg.G != 0.f;
 }
@@ -362,6 +371,7 @@ int lb_set_populations(lb_ctx *c, const float *f) {
             c->launches += 1;
         }
     }
+    LB_TRY(c, "lb_set_populations", mirror_sets(c));
     LB_TRY(c, "lb_set_populations", cudaStreamSynchronize(c->stream));
     return LB_OK;
 }
@@ -417,6 +427,7 @@ int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const floa
     }
     LB_TRY(c, "lb_init_equilibrium", e);
     c->launches += 1;
+    LB_TRY(c, "lb_init_equilibrium", mirror_sets(c));
     LB_TRY(c, "lb_init_equilibrium", cudaStreamSynchronize(c->stream));
     return LB_OK;
 }
@@ -763,6 +774,7 @@ int lb_checkpoint_load(lb_ctx *c, const char *path) {
     int rc = LB_OK;
     for (int k = 0; k < c->Q && rc == LB_OK; k++) rc = upload(pop_k(c, c->cur, k), pop_k_bytes);
     for (int i = 0; i < n_moments(c) && rc == LB_OK; i++) rc = upload(mom_k(c, i), mom_k_bytes);
+    if (rc == LB_OK && mirror_sets(c) != cudaSuccess) rc = LB_ERR_CUDA;
     fclose(fp);
     if (rc == LB_ERR_IO) return fail(c, rc, "lb_checkpoint_load: read failed");
     if (rc != LB_OK) return fail(c, rc, "lb_checkpoint_load: copy to the device failed");

@@ -16,7 +16,16 @@ STEPS = 16
 
 
 def beq(a, b):
-    return np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+    """bit-identical, except that a NaN matches any NaN: the bit pattern of a
+    NaN made by an invalid operation differs between the GPU and the host CPU
+    (two sample cases, the 0 and 90 degree contact angles, go non-finite
+    within 16 steps in the reference's own semantics)"""
+    a, b = np.asarray(a), np.asarray(b)
+    if a.dtype != np.float32:
+        return np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32),
+                                                     b[~nb].view(np.uint32))
 
 
 def distinct_2d_cases():
