@@ -168,6 +168,14 @@ typedef enum {
                                         kernel (psi halo in shared memory) instead of
                                         the separate psi pass; same results, measured
                                         slower (17.7 vs 25.9 GLUPS at 256^3) */
+#define LB_TUNE_PERSISTENT 0x004 /* D2Q9 without Shan-Chen: lb_step runs all its steps
+                                    in one cooperative launch whose blocks own row
+                                    bands and wait (bounded) only for their two
+                                    neighbour bands; for lattices whose step is
+                                    shorter than a launch */
+#define LB_TUNE_PDL 0x008      /* D2Q9 without Shan-Chen: each step is a programmatic
+                                  dependent launch of the previous one, so its launch
+                                  overlaps the previous step's tail */
 #define LB_TUNE_REVERSE 0x001  /* sweep the lattice in the opposite order on every
                                   other step, so a step starts where the previous
                                   one ended and its last writes are still in L2 */

@@ -29,6 +29,8 @@ struct lb_ctx {
     float *sc = nullptr;                 // psi (D3Q19, D2Q9) and ueq_x, ueq_y (D2Q9)
     float *stage = nullptr;              // 16-bit storage: one float array for conversions
     double *red = nullptr;               // reduction partials + result
+    int *psync = nullptr;                // D2Q9 persistent loop: error word + band step counts
+    bool persist_pending = false;        // a persistent launch whose error word is unread
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -58,9 +60,14 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
         if (e_ != cudaSuccess) return cuda_fail(c, where, e_);  \
     } while (0)
 
-// launch tuning used when the caller leaves lb_config.tuning at LB_TUNE_DEFAULT:
-// the alternating sweep measured 44.7 vs 43.8 GLUPS on the 256x128x128 channel
-constexpr int LB_TUNE_LIBRARY_DEFAULT = LB_TUNE_REVERSE;
+// launch tuning used when the caller leaves lb_config.tuning at LB_TUNE_DEFAULT.
+// D3Q19: the alternating sweep measured 44.7 vs 43.8 GLUPS on the 256x128x128
+// channel.  D2Q9: programmatic dependent launches measured 24.9 vs 22.7 GLUPS
+// on the 256^2 cavity (the alternating sweep: 23.8 with them); the persistent
+// loop measured 9.7 (each step waits on a chain of L2 round trips) and stays
+// opt-in.
+constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE;
+constexpr int LB_TUNE_LIBRARY_DEFAULT_D2 = LB_TUNE_PDL;
 
 const double W3[3] = {1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0};
 const double W2[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
@@ -108,6 +115,47 @@ bool sc_on(const lb_ctx *c) {
     return c->cfg.mode == LB_MODE_REFERENCE ? (c->Q == 9 && c->cfg.G < 0.f) : c->cfg.G != 0.f;
 }
 
+// the D2Q9 persistent step loop applies: no Shan-Chen pass and the tuning
+// asks for it
+bool persistent_on(const lb_ctx *c) {
+    return c->Q == 9 && !sc_on(c) && (c->tune & LB_TUNE_PERSISTENT);
+}
+
+// after the stream has been synchronised: the error word of the last
+// persistent launch (a block that gave up waiting for a neighbour band)
+int check_persistent(lb_ctx *c) {
+    if (!c->persist_pending) return LB_OK;
+    int word = 0;
+    LB_TRY(c, "persistent step loop",
+           cudaMemcpy(&word, c->psync, sizeof(int), cudaMemcpyDeviceToHost));
+    c->persist_pending = false;
+    if (word != 0)
+        return fail(c, LB_ERR_DEVICE,
+                    "persistent step loop: a block gave up waiting for its neighbour band");
+    return LB_OK;
+}
+
+// the D2Q9 kernel arguments of a step from set `from` into set 1-from
+D2Args d2_args(lb_ctx *c, int from) {
+    const lb_config &g = c->cfg;
+    D2Args a{};
+    for (int k = 0; k < 9; k++) {
+        a.src.f[k] = pop_k(c, from, k);
+        a.dst.f[k] = pop_k(c, 1 - from, k);
+    }
+    a.flags = c->flags; a.sb = c->sb;
+    a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
+    a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2);
+    a.psi = c->sc; a.ueq_x = c->sc + c->stride; a.ueq_y = c->sc + 2 * c->stride;
+    a.W = g.nx; a.H = g.ny; a.dev = 0; a.ndev = 1;
+    a.w0 = (float)W2[0]; a.w1 = (float)W2[1]; a.w5 = (float)W2[2];
+    a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
+    a.Fx = g.force[0]; a.Fy = g.force[1]; a.G = g.G; a.Gads = g.G_ads;
+    a.psi_form = g.psi_form;
+    memcpy(a.corr, c->corr, sizeof(float) * 9);
+    return a;
+}
+
 // one time step from set `from` into set 1-from
 cudaError_t step_once(lb_ctx *c, int from, bool moments) {
     const lb_config &g = c->cfg;
@@ -144,22 +192,11 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         c->launches += sc ? 2 : 1;
         return launch_d3q19_native(a, g.storage, moments, sc, c->stream);
     }
-    D2Args a{};
-    for (int k = 0; k < 9; k++) {
-        a.src.f[k] = pop_k(c, from, k);
-        a.dst.f[k] = pop_k(c, to, k);
-    }
-    a.flags = c->flags; a.sb = c->sb;
-    a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
-    a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2);
-    a.psi = c->sc; a.ueq_x = c->sc + c->stride; a.ueq_y = c->sc + 2 * c->stride;
-    a.W = g.nx; a.H = g.ny; a.dev = 0; a.ndev = 1;
-    a.w0 = (float)W2[0]; a.w1 = (float)W2[1]; a.w5 = (float)W2[2];
-    a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
-    a.Fx = g.force[0]; a.Fy = g.force[1]; a.G = g.G; a.Gads = g.G_ads;
-    a.psi_form = g.psi_form;
-    memcpy(a.corr, c->corr, sizeof(float) * 9);
+    const D2Args a = d2_args(c, from);
     c->launches += sc_on(c) ? 2 : 1;
+    if (!sc_on(c) && (c->tune & LB_TUNE_PDL))
+        return launch_d2q9_fused_pdl(a, g.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE,
+                                     moments, c->stream);
     return launch_d2q9_fused(a, g.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE, moments,
                              false, c->stream);
 }
@@ -282,7 +319,10 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (c->cfg.graph_steps <= 0) c->cfg.graph_steps = 64;
     c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
     if (!(c->cfg.rho_ref > 0.f)) c->cfg.rho_ref = 1.f;
-    c->tune = (cfg->tuning & LB_TUNE_EXPLICIT) ? (cfg->tuning & 0xff) : LB_TUNE_LIBRARY_DEFAULT;
+    c->tune = (cfg->tuning & LB_TUNE_EXPLICIT)
+                  ? (cfg->tuning & 0xff)
+                  : (cfg->lattice == LB_D2Q9 ? LB_TUNE_LIBRARY_DEFAULT_D2
+                                             : LB_TUNE_LIBRARY_DEFAULT_D3);
     c->Q = cfg->lattice;
     c->N = N;
     c->stride = (N + 127) / 128 * 128;  // every population array starts on a 256-byte boundary
@@ -302,6 +342,7 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (e == cudaSuccess && c->esize != 4) e = cudaMalloc(&c->stage, sizeof(float) * c->stride);
     // reduction partials, 7 results, then 4 floats (2 doubles) for lb_probe
     if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 16));
+    if (e == cudaSuccess && c->Q == 9) e = cudaMalloc(&c->psync, sizeof(int) * (cfg->ny + 1));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -332,6 +373,7 @@ int lb_destroy(lb_ctx *c) {
     if (c->sc) cudaFree(c->sc);
     if (c->stage) cudaFree(c->stage);
     if (c->red) cudaFree(c->red);
+    if (c->psync) cudaFree(c->psync);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -393,7 +435,7 @@ int lb_get_populations(lb_ctx *c, float *f) {
         // the staging array is reused by the next population
         LB_TRY(c, "lb_get_populations", cudaStreamSynchronize(c->stream));
     }
-    return LB_OK;
+    return check_persistent(c);
 }
 
 int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const float *uy,
@@ -435,6 +477,26 @@ int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const floa
 int lb_step(lb_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return fail(c, LB_ERR_ARG, "lb_step: bad argument");
     if (nsteps == 0) return LB_OK;
+    if (persistent_on(c)) {
+        // every step in one cooperative launch; falls through to the graphs
+        // when the bands cannot all be resident
+        LB_TRY(c, "lb_step", cudaMemsetAsync(c->psync, 0, sizeof(int) * (c->cfg.ny + 1),
+                                             c->stream));
+        const cudaError_t e =
+            launch_d2q9_persistent(d2_args(c, c->cur),
+                                   c->cfg.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE,
+                                   nsteps, c->psync, c->stream);
+        if (e == cudaSuccess) {
+            c->launches += 1;
+            c->persist_pending = true;
+            c->cur = (c->cur + nsteps) & 1;
+            c->steps += nsteps;
+            return LB_OK;
+        }
+        if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported)
+            return cuda_fail(c, "lb_step (persistent)", e);
+        (void)cudaGetLastError();
+    }
     int rest = nsteps - 1;  // the last step also writes the moment fields
     while (rest >= c->cfg.graph_steps) {
         cudaGraphExec_t g;
@@ -464,7 +526,7 @@ int lb_get_moments(lb_ctx *c, float *rho, float *ux, float *uy, float *uz) {
                                c->stream));
     }
     LB_TRY(c, "lb_get_moments", cudaStreamSynchronize(c->stream));
-    return LB_OK;
+    return check_persistent(c);
 }
 
 int lb_reduce(lb_ctx *c, double out[7]) {
@@ -476,7 +538,7 @@ int lb_reduce(lb_ctx *c, double out[7]) {
     c->launches += 2;
     LB_TRY(c, "lb_reduce", cudaMemcpyAsync(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
     LB_TRY(c, "lb_reduce", cudaStreamSynchronize(c->stream));
-    return LB_OK;
+    return check_persistent(c);
 }
 
 int lb_probe(lb_ctx *c, int x, int y, int z, float value[4]) {
@@ -528,7 +590,7 @@ int lb_extents(const lb_ctx *c, int *nx, int *ny, int *nz) {
 int lb_synchronize(lb_ctx *c) {
     if (!c) return LB_ERR_ARG;
     LB_TRY(c, "lb_synchronize", cudaStreamSynchronize(c->stream));
-    return LB_OK;
+    return check_persistent(c);
 }
 
 int lb_time_steps(lb_ctx *c, int nsteps, float *ms) {
@@ -539,7 +601,7 @@ int lb_time_steps(lb_ctx *c, int nsteps, float *ms) {
     LB_TRY(c, "lb_time_steps", cudaEventRecord(c->ev1, c->stream));
     LB_TRY(c, "lb_time_steps", cudaEventSynchronize(c->ev1));
     LB_TRY(c, "lb_time_steps", cudaEventElapsedTime(ms, c->ev0, c->ev1));
-    return LB_OK;
+    return check_persistent(c);
 }
 
 int64_t lb_launch_count(const lb_ctx *c) { return c ? c->launches : -1; }

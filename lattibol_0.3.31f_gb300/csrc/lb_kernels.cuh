@@ -78,6 +78,15 @@ cudaError_t launch_d3q19_equilibrium(const Pop<19> &p, const float *rho, const f
 
 // D2Q9
 cudaError_t launch_d2q9_fused(const D2Args &a, int mode, bool mom, bool plot, cudaStream_t s);
+// launch_d2q9_fused without Shan-Chen or plot, as a programmatic dependent
+// launch (the grid may start while the previous kernel on s drains)
+cudaError_t launch_d2q9_fused_pdl(const D2Args &a, int mode, bool mom, cudaStream_t s);
+// every step of a batch in one cooperative launch (small lattices, no
+// Shan-Chen); sync holds a.H + 1 zeroed ints, sync[0] != 0 afterwards means a
+// block gave up waiting for a neighbour band.  cudaErrorCooperativeLaunchTooLarge
+// when the bands cannot all be resident.
+cudaError_t launch_d2q9_persistent(const D2Args &a, int mode, int nsteps, int *sync,
+                                   cudaStream_t s);
 cudaError_t launch_d2q9_stream_swap(const Pop<9> &p, const uint8_t *sb, int W, int H,
                                     cudaStream_t s);
 cudaError_t launch_d2q9_collide(const D2Args &a, bool plot, cudaStream_t s);
