@@ -505,11 +505,13 @@ def main():
 def measure_e2e(pkg, L, wl, flags, steps, ws, dist):
     """End to end through the library's C ABI with host buffers: the initial
     populations are uploaded from pinned host memory (lb_set_populations),
-    then lb_run_probe runs the reference's per-step host pattern (one step
-    that writes the moment fields, then a read_value-style probe of one node
-    copied to the host and waited for, every step), and the final rho and u
-    fields are read back into pinned host memory -- all inside the timed
-    region.  Same workload and physics as the device-resident number."""
+    then lb_run_probe runs the reference's per-step host pattern (a step,
+    then the read_value-style cursor value delivered to host memory -- here
+    written by every step's kernel into mapped page-locked memory, so the
+    steps replay from CUDA graphs without a host round trip between them),
+    and the final rho and u fields are read back into pinned host memory --
+    all inside the timed region.  Same workload and physics as the
+    device-resident number."""
     import ctypes as C
     N = wl.N
     nx, ny, nz = wl.size
@@ -560,8 +562,9 @@ def measure_e2e(pkg, L, wl, flags, steps, ws, dist):
     return {"value": ws * N * steps / el / 1e9, "unit": "GLUPS",
             "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
             "steps": steps, "gpu_launches": launches,
-            "path": "lb_set_populations + lb_run_probe (step with moments, 16-byte probe copy "
-                    "each step) + lb_get_moments, pinned host buffers, wall clock"}
+            "path": "lb_set_populations + lb_run_probe (every step's kernel writes the cursor's "
+                    "16 bytes into mapped pinned host memory; graph-replayed steps) + "
+                    "lb_get_moments, pinned host buffers, wall clock"}
 
 
 if __name__ == "__main__":

@@ -223,9 +223,12 @@ int lb_reduce(lb_ctx *ctx, double out[7]);
 /* (ux, uy, uz, rho) of the last step at one node, copied to host memory
  * (blocks until the copy is done) -- the context form of read_value_3d */
 int lb_probe(lb_ctx *ctx, int x, int y, int z, float value[4]);
-/* the reference's per-step host pattern on a context: nsteps times one step
- * that writes the moment fields, then lb_probe at (x, y, z); value[4] holds
- * the last probe */
+/* the reference's per-step host pattern on a context (a step, then the
+ * cursor value read to the host): every step's kernel writes (ux, uy, uz, rho)
+ * of node (x, y, z) into mapped page-locked host memory, so the steps replay
+ * from graphs without a host round trip between them; value[4] holds the last
+ * step's, the moment fields the last step's.  (The closure and single-pass
+ * Shan-Chen kernels fall back to a step plus lb_probe per step.) */
 int lb_run_probe(lb_ctx *ctx, int nsteps, int x, int y, int z, float value[4]);
 int lb_synchronize(lb_ctx *ctx);
 /* run nsteps and return the device time between CUDA events recorded on the

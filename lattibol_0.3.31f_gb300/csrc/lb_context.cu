@@ -30,6 +30,9 @@ struct lb_ctx {
     float *stage = nullptr;              // 16-bit storage: one float array for conversions
     double *red = nullptr;               // reduction partials + result
     int *psync = nullptr;                // D2Q9 persistent loop: error word + band step counts
+    float4 *probe_host = nullptr;        // lb_run_probe: mapped page-locked cursor value
+    float4 *probe_dev = nullptr;         // its device address
+    int probe_o = -1;                    // cursor node the captured graphs write (-1: none)
     bool persist_pending = false;        // a persistent launch whose error word is unread
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
@@ -121,6 +124,24 @@ bool persistent_on(const lb_ctx *c) {
     return c->Q == 9 && !sc_on(c) && (c->tune & LB_TUNE_PERSISTENT);
 }
 
+// the step kernels write the cursor probe themselves on every path except the
+// closure kernel and the single-pass Shan-Chen kernel
+bool probe_in_step(const lb_ctx *c) {
+    if (c->Q == 9) return true;
+    if (c->closure_on) return false;
+    return !(c->cfg.mode == LB_MODE_NATIVE && sc_on(c) && (c->tune & LB_TUNE_SC_SINGLE_PASS) &&
+             sc_march_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz));
+}
+
+// forget the captured step graphs (their kernel arguments changed)
+void drop_graphs(lb_ctx *c) {
+    for (int i = 0; i < 2; i++)
+        if (c->graph[i]) {
+            cudaGraphExecDestroy(c->graph[i]);
+            c->graph[i] = nullptr;
+        }
+}
+
 // after the stream has been synchronised: the error word of the last
 // persistent launch (a block that gave up waiting for a neighbour band)
 int check_persistent(lb_ctx *c) {
@@ -153,6 +174,8 @@ D2Args d2_args(lb_ctx *c, int from) {
     a.Fx = g.force[0]; a.Fy = g.force[1]; a.G = g.G; a.Gads = g.G_ads;
     a.psi_form = g.psi_form;
     memcpy(a.corr, c->corr, sizeof(float) * 9);
+    a.probe = c->probe_o >= 0 ? c->probe_dev : nullptr;
+    a.probe_o = c->probe_o;
     return a;
 }
 
@@ -176,6 +199,8 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         memcpy(a.corr, c->corr, sizeof(a.corr));
         memcpy(a.wr, c->wr, sizeof(a.wr));
         a.psi = c->sc; a.G = g.G; a.psi_form = g.psi_form;
+        a.probe = c->probe_o >= 0 ? c->probe_dev : nullptr;
+        a.probe_o = c->probe_o;
         if (g.mode == LB_MODE_REFERENCE) {
             c->launches += 1;
             return launch_d3q19_fused(a, MODE_REF, moments, false, c->stream);
@@ -374,6 +399,7 @@ int lb_destroy(lb_ctx *c) {
     if (c->stage) cudaFree(c->stage);
     if (c->red) cudaFree(c->red);
     if (c->psync) cudaFree(c->psync);
+    if (c->probe_host) cudaFreeHost(c->probe_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -560,6 +586,33 @@ int lb_probe(lb_ctx *c, int x, int y, int z, float value[4]) {
 
 int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
     if (!c || !value || nsteps < 0) return LB_ERR_ARG;
+    if (x < 0 || y < 0 || z < 0 || x >= c->cfg.nx || y >= c->cfg.ny || z >= c->cfg.nz)
+        return fail(c, LB_ERR_ARG, "lb_run_probe: node outside the lattice");
+    if (nsteps == 0) return LB_OK;
+    if (probe_in_step(c)) {
+        // every step's kernel writes the cursor node's moments into mapped
+        // page-locked memory: the steps replay from graphs with no host
+        // round trip between them
+        if (!c->probe_host) {
+            LB_TRY(c, "lb_run_probe",
+                   cudaHostAlloc((void **)&c->probe_host, sizeof(float4), cudaHostAllocMapped));
+            LB_TRY(c, "lb_run_probe",
+                   cudaHostGetDevicePointer((void **)&c->probe_dev, c->probe_host, 0));
+        }
+        const int o = x + c->cfg.nx * (y + c->cfg.ny * z);
+        if (o != c->probe_o) {
+            LB_TRY(c, "lb_run_probe", cudaStreamSynchronize(c->stream));
+            drop_graphs(c);  // the captured steps carry the probe node
+            c->probe_o = o;
+        }
+        int rc = lb_step(c, nsteps);
+        if (rc != LB_OK) return rc;
+        LB_TRY(c, "lb_run_probe", cudaStreamSynchronize(c->stream));
+        rc = check_persistent(c);
+        if (rc != LB_OK) return rc;
+        memcpy(value, (const void *)c->probe_host, 4 * sizeof(float));
+        return LB_OK;
+    }
     for (int i = 0; i < nsteps; i++) {
         LB_TRY(c, "lb_run_probe", step_once(c, c->cur, true));
         c->cur = 1 - c->cur;
@@ -946,11 +999,7 @@ int lb::context_set_closure(lb_ctx *c, const ClosureArgs *ca) {
                sc_on(c)))
         return fail(c, LB_ERR_ARG, "closure: D3Q19 native mode, FP32 storage, no Shan-Chen");
     LB_TRY(c, "closure", cudaStreamSynchronize(c->stream));
-    for (int i = 0; i < 2; i++)
-        if (c->graph[i]) {
-            cudaGraphExecDestroy(c->graph[i]);
-            c->graph[i] = nullptr;
-        }
+    drop_graphs(c);
     c->closure_on = ca != nullptr;
     if (ca) c->closure = *ca;
     return LB_OK;

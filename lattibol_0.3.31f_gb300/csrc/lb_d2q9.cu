@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
             a.psi[o] = 0.f;
         }
         if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.rho[o] = 0.f; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
 
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
     if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
     if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
     if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
+    if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
     if (SC) {
         a.psi[o] = (MODE == MODE_REF || a.psi_form == 0) ? psi_ref(rho) : psi_exp1(rho);
         a.ueq_x[o] = ex;
@@ -309,6 +311,7 @@ __device__ __forceinline__ void d2q9_node_l2(const D2Args &a, int par, int x, in
             }
         }
         if (mom) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.rho[o] = 0.f; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     float g[9];
@@ -340,6 +343,7 @@ __device__ __forceinline__ void d2q9_node_l2(const D2Args &a, int par, int x, in
     if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
     if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
     if (mom) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
+    if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
     d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, a.tau_inv);
 #pragma unroll
     for (int k = 0; k < 9; k++) dst[k][o] = g[k];

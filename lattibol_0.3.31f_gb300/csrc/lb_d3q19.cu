@@ -55,10 +55,12 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
         }
         if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
         if (PLOT) a.plot[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     if (MODE == MODE_NATIVE && (fl & CELL_WALL)) {
         if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
 
@@ -78,6 +80,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
     d3q19_moments(g, rho, ux, uy, uz);
     if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
     if (PLOT) a.plot[o] = make_float4(ux, uy, uz, rho);
+    if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
     float ex = ux, ey = uy, ez = uz;
     if (MODE == MODE_NATIVE) {
         // velocity-shift forcing, the form of reference src/collision.cu:280-284

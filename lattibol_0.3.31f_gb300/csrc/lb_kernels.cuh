@@ -28,6 +28,8 @@ struct D3Args {
     float *psi;             // Shan-Chen: pseudo-potential of the current step (density pass)
     float G;                // Shan-Chen interaction strength
     int psi_form;           // LB_PSI_REF or LB_PSI_EXP1
+    float4 *probe;          // when set: (ux, uy, uz, rho) of node probe_o, every step
+    int probe_o;            // (mapped host memory: the cursor read without a sync)
 };
 
 struct D2Args {
@@ -43,6 +45,8 @@ struct D2Args {
     float w0, w1, w5, tau_inv, ux_in, rho_out, Fx, Fy, G, Gads;
     int psi_form;
     float corr[9];
+    float4 *probe;          // as D3Args: (ux, uy, 0, rho) of node probe_o every step
+    int probe_o;
 };
 
 // D3Q19
