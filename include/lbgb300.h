@@ -313,6 +313,10 @@ int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_
 /* device pointers of a context's moment fields (valid until lb_destroy) and
  * its extents */
 int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **uz);
+/* self-check of the tensor-core (tcgen05) operand layout the closure kernel
+ * uses: out[128][64] = X W^T with X[r][k] = (7r + 3k) mod 9 - 4 and
+ * W[n][k] = (5n + k) mod 7 - 3, k < 32 (exact small integers) */
+int lb_tcgen05_selftest(float *out);
 int lb_extents(const lb_ctx *ctx, int *nx, int *ny, int *nz);
 
 /* ======================================================================== */
