@@ -173,6 +173,9 @@ typedef enum {
                                     bands and wait (bounded) only for their two
                                     neighbour bands; for lattices whose step is
                                     shorter than a launch */
+#define LB_TUNE_CLOSURE_MMA_SYNC 0x010 /* learned closure: evaluate the network with the
+                                          warp-level mma.sync kernel instead of the
+                                          tcgen05 (tensor memory) kernel */
 #define LB_TUNE_PDL 0x008      /* D2Q9 without Shan-Chen: each step is a programmatic
                                   dependent launch of the previous one, so its launch
                                   overlaps the previous step's tail */
@@ -313,10 +316,13 @@ int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_
 /* device pointers of a context's moment fields (valid until lb_destroy) and
  * its extents */
 int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **uz);
-/* self-check of the tensor-core (tcgen05) operand layout the closure kernel
- * uses: out[128][64] = X W^T with X[r][k] = (7r + 3k) mod 9 - 4 and
- * W[n][k] = (5n + k) mod 7 - 3, k < 32 (exact small integers) */
-int lb_tcgen05_selftest(float *out);
+/* self-check of the tensor-core (tcgen05) pattern the closure kernel uses, in
+ * one CTA, three rounds: out[round][0] (128 x 64) = X W1^T with
+ * X[r][k] = ((7r + 3k) mod 9 - 4)(round + 1), W1[n][k] = (5n + k) mod 7 - 3,
+ * k < 32; out[round][1] = H W2^T with H[r][k] = (r + 3k + round) mod 5 - 2,
+ * W2[n][k] = (n + 2k) mod 5 - 2, k < 64 (exact small integers).  *status
+ * gets bit 2i (bit 2i+1) when round i's first (second) MMA never completed. */
+int lb_tcgen05_selftest(float *out, int *status);
 int lb_extents(const lb_ctx *ctx, int *nx, int *ny, int *nz);
 
 /* ======================================================================== */

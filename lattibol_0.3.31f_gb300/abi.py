@@ -94,7 +94,7 @@ LB_PSI_REF, LB_PSI_EXP1 = 0, 1
 LB_CELL_FLUID, LB_CELL_WALL, LB_CELL_MOVING = 0, 1, 2
 LB_ABI_STANDALONE, LB_ABI_FUSED = 0, 1
 LB_TUNE_DEFAULT, LB_TUNE_EXPLICIT, LB_TUNE_REVERSE, LB_TUNE_SC_SINGLE_PASS = 0, 0x100, 0x001, 0x002
-LB_TUNE_PERSISTENT, LB_TUNE_PDL = 0x004, 0x008
+LB_TUNE_PERSISTENT, LB_TUNE_PDL, LB_TUNE_CLOSURE_MMA_SYNC = 0x004, 0x008, 0x010
 
 _c = ctypes
 # (name, restype, argtypes) of every exported C symbol declared in include/lbgb300.h
@@ -177,7 +177,7 @@ PROTOTYPES = [
                                      _c.c_void_p, _c.c_void_p, _c.POINTER(_c.c_double)]),
     ("lb_device_fields", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_void_p)] * 4),
     ("lb_extents", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3),
-    ("lb_tcgen05_selftest", _c.c_int, [_c.c_void_p]),
+    ("lb_tcgen05_selftest", _c.c_int, [_c.c_void_p, _c.POINTER(_c.c_int)]),
     ("lb_case_load_parameters", _c.c_int, [_c.c_char_p, _c.POINTER(lb_case_params)]),
     ("lb_case_load_solids_bmp", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_int),
                                            _c.POINTER(_c.c_int), _c.c_void_p, _c.c_size_t]),

@@ -18,6 +18,7 @@
 // * training: the forward pass of the closure kernel (tensor cores), an FP32
 //   backward pass per sample, per-block weight-gradient sums in shared
 //   memory, a fixed-order reduction of the block partials, and Adam.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -25,6 +26,7 @@
 
 #include "../../include/lbgb300.h"
 #include "lb_d3q19.cuh"
+#include "lb_tc05.cuh"
 
 using namespace lb;
 
@@ -115,12 +117,14 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
         if (!inside) continue;
         if (!fluid) {
             if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
         }
         if (ca.y_out) ca.y_out[o] = yv;
         const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
         const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
         if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
         float ex = ux, ey = uy, ez = uz;
         if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
         if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
@@ -131,8 +135,211 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same step with the network on the 5th-generation tensor cores.  A block
+// of 128 threads takes a run of 128 cells; thread t owns cell t, row t of the
+// MMA tiles and lane t of tensor memory.  Per run:
+//   1. every thread writes its 19 BF16 features (padded to 32) as row t of A
+//      (K-major 8x8 core matrices, lb_tc05.cuh);
+//   2. thread 0 issues D = A W1^T (M 128, N 64, two k16 MMAs, FP32 in 64
+//      tensor-memory columns) and commits to an mbarrier;
+//   3. each warp loads its 32 lanes of D, adds b1, applies ReLU and writes the
+//      BF16 hidden row over A (now K = 64);
+//   4. thread 0 issues D = H W2^T (four k16 MMAs) into the same columns;
+//   5. each thread loads its row, adds b2, applies ReLU and sums w3 h + b3.
+// Rounding points are the warp-level kernel's (BF16 inputs, weights and
+// first hidden layer; FP32 accumulation, biases and last layer).
+// ---------------------------------------------------------------------------
+constexpr int TC_COLS = 64;             // tensor-memory columns per block (D is 128 x 64)
+constexpr int TC_WAIT = 1 << 22;        // mbarrier polls before a block gives up
+
+struct TcSmem {
+    uint8_t a[128 * MLP_H * 2];         // A: features (K 32) then the hidden layer (K 64)
+    uint8_t w1[MLP_H * MLP_IN_PAD * 2]; // W1 [64][32], K-major core matrices
+    uint8_t w2[MLP_H * MLP_H * 2];      // W2 [64][64]
+    float b1[MLP_H], b2[MLP_H], w3[MLP_H], b3;
+    uint64_t mbar;
+    uint32_t tslot;
+};
+
+template <bool MOM>
+__global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args a,
+                                                                    const ClosureArgs ca) {
+    __shared__ __align__(1024) TcSmem sm;
+    const int t = threadIdx.x, warp = t >> 5;
+    for (int i = t; i < MLP_H * MLP_IN_PAD; i += D3_BLOCK)
+        *reinterpret_cast<__nv_bfloat16 *>(sm.w1 + kmajor_offset(i / MLP_IN_PAD, i % MLP_IN_PAD,
+                                                                 MLP_IN_PAD)) = ca.mlp.w1[i];
+    for (int i = t; i < MLP_H * MLP_H; i += D3_BLOCK)
+        *reinterpret_cast<__nv_bfloat16 *>(sm.w2 + kmajor_offset(i / MLP_H, i % MLP_H, MLP_H)) =
+            ca.mlp.w2[i];
+    for (int i = t; i < MLP_H; i += D3_BLOCK) {
+        sm.b1[i] = ca.mlp.b1[i];
+        sm.b2[i] = ca.mlp.b2[i];
+        sm.w3[i] = ca.mlp.w3[i];
+    }
+    if (t == 0) {
+        sm.b3 = ca.mlp.b3[0];
+        mbar_init(&sm.mbar, 1);
+    }
+    if (warp == 0) tc_alloc(&sm.tslot, TC_COLS);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sm.tslot;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t a_addr = smem_u32(sm.a), w1_addr = smem_u32(sm.w1), w2_addr = smem_u32(sm.w2);
+    constexpr uint32_t id = tc_idesc_bf16(128, MLP_H);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
+    const long nrows = (long)nbx * a.H * a.D;
+    for (long r = blockIdx.x; r < nrows && ok; r += gridDim.x) {
+        const long rr = a.reverse ? nrows - 1 - r : r;
+        const int bx = (int)(rr % nbx);
+        const long yz = rr / nbx;
+        const int y = (int)(yz % a.H), z = (int)(yz / a.H);
+        const int x = bx * D3_BLOCK + t;
+        const bool inside = x < a.W;
+        const int o = inside ? x + a.W * (y + a.H * z) : 0;
+        const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
+        const bool fluid = !(fl & CELL_WALL);
+        float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        float feat[MLP_IN];
+#pragma unroll
+        for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
+        if (fluid) {
+            const Nbr3 n(x, y, z, a.W, a.H, a.D);
+            pull_native<float>(a, o, n, fl, g);
+            d3q19_moments(g, rho, ux, uy, uz);
+            closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
+        }
+        // 1. features -> row t of A (four 16-byte column groups, K = 32)
+#pragma unroll
+        for (int h = 0; h < MLP_IN_PAD / 8; h++) {
+            __nv_bfloat162 p[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int k0 = 8 * h + 2 * j;
+                p[j] = __floats2bfloat162_rn(k0 < MLP_IN ? feat[k0] : 0.f,
+                                             k0 + 1 < MLP_IN ? feat[k0 + 1] : 0.f);
+            }
+            *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, 8 * h, MLP_IN_PAD)) =
+                *reinterpret_cast<const uint4 *>(p);
+        }
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        // 2. layer 1
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int s = 0; s < MLP_IN_PAD / 16; s++)
+                tc_mma_bf16(tmem, tc_desc(a_addr + 256 * s, 128, MLP_IN_PAD / 8 * 128),
+                            tc_desc(w1_addr + 256 * s, 128, MLP_IN_PAD / 8 * 128), id, s > 0);
+            tc_commit(&sm.mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(&sm.mbar, phase, TC_WAIT));
+        phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        // 3. hidden layer: + b1, ReLU, BF16 -> row t of A (K = 64)
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + (uint32_t)c, v);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                __nv_bfloat162 p[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int q = 8 * h + 2 * j;
+                    p[j] = __floats2bfloat162_rn(fmaxf(v[q] + sm.b1[c + q], 0.f),
+                                                 fmaxf(v[q + 1] + sm.b1[c + q + 1], 0.f));
+                }
+                *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, c + 8 * h, MLP_H)) =
+                    *reinterpret_cast<const uint4 *>(p);
+            }
+        }
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        // 4. layer 2
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int s = 0; s < MLP_H / 16; s++)
+                tc_mma_bf16(tmem, tc_desc(a_addr + 256 * s, 128, MLP_H / 8 * 128),
+                            tc_desc(w2_addr + 256 * s, 128, MLP_H / 8 * 128), id, s > 0);
+            tc_commit(&sm.mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(&sm.mbar, phase, TC_WAIT));
+        phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        // 5. output: b3 + sum_j w3_j ReLU(D_j + b2_j)
+        float yv = 0.f;
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 32; j++) yv = yv + sm.w3[c + j] * fmaxf(v[j] + sm.b2[c + j], 0.f);
+        }
+        yv = yv + sm.b3;
+        tc_fence_before();  // the next run's MMA overwrites these columns after a barrier
+        if (!inside) continue;
+        if (!fluid) {
+            if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        if (ca.y_out) ca.y_out[o] = yv;
+        const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
+        const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
+        if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
+        float ex = ux, ey = uy, ez = uz;
+        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
+        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
+        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
+        d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+#pragma unroll
+        for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+    }
+    if (!ok) {
+        // an MMA did not complete: record it, give it one more bounded wait so
+        // that no MMA is writing the columns when they are released
+        if (t == 0 && ca.err) atomicExch(ca.err, 1);
+        mbar_wait(&sm.mbar, phase ^ 1, TC_WAIT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, TC_COLS);
+    if (t == 0) mbar_inval(&sm.mbar);
+}
+
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s) {
+    if (!ca.legacy_mma) {
+        // SMs x resident blocks, at most 8 per SM (8 x 64 tensor-memory columns)
+        static int tc_cap = 0;
+        if (!tc_cap) {
+            int dev = 0, sms = 1, occ = 1;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, d3q19_closure_tc_kernel<false>,
+                                                          D3_BLOCK, 0);
+            tc_cap = sms * std::min(std::max(occ, 1), 512 / TC_COLS);
+        }
+        const long nrows = (long)((a.W + D3_BLOCK - 1) / D3_BLOCK) * a.H * a.D;
+        const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
+        if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
+        else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
+        return cudaGetLastError();
+    }
     static int grid_cap = 0;  // SMs x resident blocks of the kernel, computed once
     if (!grid_cap) {
         int dev = 0, sms = 1, occ = 1;

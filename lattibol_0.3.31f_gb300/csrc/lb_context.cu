@@ -125,10 +125,10 @@ bool persistent_on(const lb_ctx *c) {
 }
 
 // the step kernels write the cursor probe themselves on every path except the
-// closure kernel and the single-pass Shan-Chen kernel
+// single-pass Shan-Chen kernel
 bool probe_in_step(const lb_ctx *c) {
     if (c->Q == 9) return true;
-    if (c->closure_on) return false;
+    if (c->closure_on) return true;
     return !(c->cfg.mode == LB_MODE_NATIVE && sc_on(c) && (c->tune & LB_TUNE_SC_SINGLE_PASS) &&
              sc_march_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz));
 }
@@ -142,17 +142,20 @@ void drop_graphs(lb_ctx *c) {
         }
 }
 
-// after the stream has been synchronised: the error word of the last
-// persistent launch (a block that gave up waiting for a neighbour band)
+// after the stream has been synchronised: the device error word written by
+// the kernels that wait on the GPU (a persistent D2Q9 block that gave up
+// waiting for a neighbour band; a tcgen05 closure MMA that never completed)
 int check_persistent(lb_ctx *c) {
     if (!c->persist_pending) return LB_OK;
     int word = 0;
-    LB_TRY(c, "persistent step loop",
+    LB_TRY(c, "device error word",
            cudaMemcpy(&word, c->psync, sizeof(int), cudaMemcpyDeviceToHost));
     c->persist_pending = false;
-    if (word != 0)
+    if (word != 0) {
+        LB_TRY(c, "device error word", cudaMemset(c->psync, 0, sizeof(int)));
         return fail(c, LB_ERR_DEVICE,
-                    "persistent step loop: a block gave up waiting for its neighbour band");
+                    "a kernel gave up waiting on the GPU (persistent band or tensor-core MMA)");
+    }
     return LB_OK;
 }
 
@@ -207,7 +210,11 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         }
         if (c->closure_on) {
             c->launches += 1;
-            return launch_d3q19_closure(a, c->closure, moments, c->stream);
+            ClosureArgs ca = c->closure;
+            ca.err = c->psync;
+            ca.legacy_mma = (c->tune & LB_TUNE_CLOSURE_MMA_SYNC) ? 1 : 0;
+            c->persist_pending = true;  // the tcgen05 kernel reports through psync[0]
+            return launch_d3q19_closure(a, ca, moments, c->stream);
         }
         const bool sc = sc_on(c);
         if (sc && (c->tune & LB_TUNE_SC_SINGLE_PASS) && sc_march_chunk(g.nx, g.ny, g.nz)) {
@@ -367,7 +374,9 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (e == cudaSuccess && c->esize != 4) e = cudaMalloc(&c->stage, sizeof(float) * c->stride);
     // reduction partials, 7 results, then 4 floats (2 doubles) for lb_probe
     if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 16));
-    if (e == cudaSuccess && c->Q == 9) e = cudaMalloc(&c->psync, sizeof(int) * (cfg->ny + 1));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&c->psync, sizeof(int) * (c->Q == 9 ? cfg->ny + 1 : 1));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->psync, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);

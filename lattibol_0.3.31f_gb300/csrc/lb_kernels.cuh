@@ -127,7 +127,9 @@ void abi_record_error(const char *where, const char *what);
 struct ClosureArgs {
     MlpDev mlp;
     float nu0, tau0, s_ref, z_max;
-    float *y_out;  // optional: network output per cell (tests)
+    float *y_out;     // optional: network output per cell (tests)
+    int *err;         // device error word (tcgen05 kernel: an MMA that never completed)
+    int legacy_mma;   // 1: the warp-level mma.sync kernel instead of tcgen05
 };
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s);

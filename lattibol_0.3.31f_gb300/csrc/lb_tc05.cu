@@ -1,8 +1,10 @@
-// lb_tc05.cu -- a self-check of the tcgen05 operand layout the closure kernel
-// uses: one CTA multiplies a 128x32 BF16 tile by a 64x32 BF16 tile
-// (D = X W^T, FP32 accumulator in tensor memory, two k16 MMAs) and writes D.
-// The operands are small integers, so the product is exact and comparable
-// bit for bit with a host product.
+// lb_tc05.cu -- a self-check of the tcgen05 pattern the closure kernel uses,
+// in one CTA of 128 threads: per round, the A tile (128 x 32 BF16) is
+// written, D = A W1^T is computed (two k16 MMAs, FP32 in 64 tensor-memory
+// columns) and read back, a hidden tile H (128 x 64 BF16, K = 64) is written
+// over A, D = H W2^T is computed into the same columns and read back.  Three
+// rounds reuse the columns and cycle the mbarrier phases as consecutive
+// cell runs do.  The operands are small integers, so every product is exact.
 #include <cuda_bf16.h>
 
 #include "../../include/lbgb300.h"
@@ -11,47 +13,94 @@
 
 namespace lb {
 
-__host__ __device__ constexpr int selftest_x(int r, int k) { return (r * 7 + k * 3) % 9 - 4; }
-__host__ __device__ constexpr int selftest_w(int n, int k) { return (n * 5 + k) % 7 - 3; }
+constexpr int ST_ROUNDS = 3;
+__host__ __device__ constexpr int selftest_x(int r, int k, int round) {
+    return ((r * 7 + k * 3) % 9 - 4) * (round + 1);
+}
+__host__ __device__ constexpr int selftest_w1(int n, int k) { return (n * 5 + k) % 7 - 3; }
+__host__ __device__ constexpr int selftest_h(int r, int k, int round) {
+    return (r + 3 * k + round) % 5 - 2;
+}
+__host__ __device__ constexpr int selftest_w2(int n, int k) { return (n + 2 * k) % 5 - 2; }
 
 __global__ void __launch_bounds__(128) tc05_selftest_kernel(float *out, int *status) {
-    __shared__ __align__(1024) uint8_t sx[128 * 32 * 2];
-    __shared__ __align__(1024) uint8_t sw[64 * 32 * 2];
+    __shared__ __align__(1024) uint8_t sa[128 * 64 * 2];
+    __shared__ __align__(1024) uint8_t sw1[64 * 32 * 2];
+    __shared__ __align__(1024) uint8_t sw2[64 * 64 * 2];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
     const int t = threadIdx.x, warp = t >> 5;
-    for (int i = t; i < 128 * 32; i += 128)
-        *reinterpret_cast<__nv_bfloat16 *>(sx + kmajor_offset(i / 32, i % 32, 32)) =
-            __float2bfloat16((float)selftest_x(i / 32, i % 32));
     for (int i = t; i < 64 * 32; i += 128)
-        *reinterpret_cast<__nv_bfloat16 *>(sw + kmajor_offset(i / 32, i % 32, 32)) =
-            __float2bfloat16((float)selftest_w(i / 32, i % 32));
+        *reinterpret_cast<__nv_bfloat16 *>(sw1 + kmajor_offset(i / 32, i % 32, 32)) =
+            __float2bfloat16((float)selftest_w1(i / 32, i % 32));
+    for (int i = t; i < 64 * 64; i += 128)
+        *reinterpret_cast<__nv_bfloat16 *>(sw2 + kmajor_offset(i / 64, i % 64, 64)) =
+            __float2bfloat16((float)selftest_w2(i / 64, i % 64));
     if (warp == 0) tc_alloc(&tslot, 64);
     if (t == 0) mbar_init(&mbar, 1);
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = tslot;
-    if (t == 0) {
-        const uint32_t idesc = tc_idesc_bf16(128, 64);
-        for (int s = 0; s < 2; s++)
-            tc_mma_bf16(tmem, tc_desc(smem_u32(sx) + 256 * s, 128, 512),
-                        tc_desc(smem_u32(sw) + 256 * s, 128, 512), idesc, s > 0);
-        tc_commit(&mbar);
-    }
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(&mbar, 0, 1 << 20));
-    tc_fence_after();
-    if (ok) {
+    const uint32_t tmem = tslot, lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t idesc = tc_idesc_bf16(128, 64);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int round = 0; round < ST_ROUNDS && ok; round++) {
+        for (int k = 0; k < 32; k++)  // row t of A
+            *reinterpret_cast<__nv_bfloat16 *>(sa + kmajor_offset(t, k, 32)) =
+                __float2bfloat16((float)selftest_x(t, k, round));
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            for (int s = 0; s < 2; s++)
+                tc_mma_bf16(tmem, tc_desc(smem_u32(sa) + 256 * s, 128, 512),
+                            tc_desc(smem_u32(sw1) + 256 * s, 128, 512), idesc, s > 0);
+            tc_commit(&mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(&mbar, phase, 1 << 20));
+        phase ^= 1;
+        if (!ok) {
+            if (t == 0) atomicOr(status, 1 << (2 * round));
+            break;
+        }
+        tc_fence_after();
         float v[32];
         for (int c = 0; c < 64; c += 32) {
-            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            tc_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
-            for (int j = 0; j < 32; j++) out[t * 64 + c + j] = v[j];
+            for (int j = 0; j < 32; j++) out[(round * 2 * 128 + t) * 64 + c + j] = v[j];
         }
-    } else if ((t & 31) == 0) {
-        atomicExch(status, 1);
+        for (int k = 0; k < 64; k++)  // row t of H over A
+            *reinterpret_cast<__nv_bfloat16 *>(sa + kmajor_offset(t, k, 64)) =
+                __float2bfloat16((float)selftest_h(t, k, round));
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            for (int s = 0; s < 4; s++)
+                tc_mma_bf16(tmem, tc_desc(smem_u32(sa) + 256 * s, 128, 1024),
+                            tc_desc(smem_u32(sw2) + 256 * s, 128, 1024), idesc, s > 0);
+            tc_commit(&mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(&mbar, phase, 1 << 20));
+        phase ^= 1;
+        if (!ok) {
+            if (t == 0) atomicOr(status, 2 << (2 * round));
+            break;
+        }
+        tc_fence_after();
+        for (int c = 0; c < 64; c += 32) {
+            tc_ld32(lane_base + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 32; j++) out[((round * 2 + 1) * 128 + t) * 64 + c + j] = v[j];
+        }
+        tc_fence_before();
     }
+    if (!ok) mbar_wait(&mbar, phase ^ 1, 1 << 20);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tc_dealloc(tmem, 64);
@@ -60,30 +109,26 @@ __global__ void __launch_bounds__(128) tc05_selftest_kernel(float *out, int *sta
 
 }  // namespace lb
 
-extern "C" int lb_tcgen05_selftest(float *out_host) {
-    if (!out_host) return LB_ERR_ARG;
+extern "C" int lb_tcgen05_selftest(float *out_host, int *status_host) {
+    if (!out_host || !status_host) return LB_ERR_ARG;
+    const size_t n = (size_t)lb::ST_ROUNDS * 2 * 128 * 64;
     float *out = nullptr;
     int *status = nullptr;
-    cudaError_t e = cudaMalloc(&out, sizeof(float) * 128 * 64);
+    cudaError_t e = cudaMalloc(&out, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(out, 0, sizeof(float) * n);
     if (e == cudaSuccess) {
         lb::tc05_selftest_kernel<<<1, 128>>>(out, status);
         e = cudaGetLastError();
     }
-    int st = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(out_host, out, sizeof(float) * 128 * 64,
-                                         cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(&st, status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_host, out, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(status_host, status, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(out);
     cudaFree(status);
     if (e != cudaSuccess) {
         lb::abi_record_error("lb_tcgen05_selftest", cudaGetErrorString(e));
         return LB_ERR_CUDA;
-    }
-    if (st) {
-        lb::abi_record_error("lb_tcgen05_selftest", "the MMA did not complete in time");
-        return LB_ERR_DEVICE;
     }
     return LB_OK;
 }

@@ -1,6 +1,7 @@
-"""GPU: the tcgen05 operand layout (K-major core matrices, shared-memory
-descriptors, BF16 MMA into tensor memory, tensor-memory loads) on a product
-whose exact value the host knows."""
+"""GPU: the tcgen05 pattern of the closure kernel (K-major core-matrix
+operands, shared-memory descriptors, BF16 MMAs into tensor memory, commit to
+an mbarrier, tensor-memory loads, a second layer over the first's columns,
+several rounds) on products whose exact values the host knows."""
 import ctypes
 
 import numpy as np
@@ -9,12 +10,19 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_tcgen05_layout_selftest(pkg):
+def test_tcgen05_selftest_rounds(pkg):
     L = pkg.lib()
-    out = np.full((128, 64), np.nan, np.float32)
-    rc = L.lb_tcgen05_selftest(out.ctypes.data_as(ctypes.c_void_p))
+    out = np.full((3, 2, 128, 64), np.nan, np.float32)
+    status = ctypes.c_int(-1)
+    rc = L.lb_tcgen05_selftest(out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(status))
     assert rc == 0, L.lb_abi_last_error()
-    r, k, n = np.arange(128)[:, None], np.arange(32)[None, :], np.arange(64)[:, None]
-    X = ((r * 7 + k * 3) % 9 - 4).astype(np.float64)
-    W = ((n * 5 + k) % 7 - 3).astype(np.float64)
-    assert np.array_equal(out, (X @ W.T).astype(np.float32))
+    assert status.value == 0
+    r, n = np.arange(128)[:, None], np.arange(64)[:, None]
+    k32, k64 = np.arange(32)[None, :], np.arange(64)[None, :]
+    W1 = ((n * 5 + k32) % 7 - 3).astype(np.float64)
+    W2 = ((n + 2 * k64) % 5 - 2).astype(np.float64)
+    for rd in range(3):
+        X = (((r * 7 + k32 * 3) % 9 - 4) * (rd + 1)).astype(np.float64)
+        H = ((r + 3 * k64 + rd) % 5 - 2).astype(np.float64)
+        assert np.array_equal(out[rd, 0], (X @ W1.T).astype(np.float32)), rd
+        assert np.array_equal(out[rd, 1], (H @ W2.T).astype(np.float32)), rd
