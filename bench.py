@@ -223,9 +223,11 @@ def run_closure(args, dist, ws, rank, local):
     train_seconds = time.perf_counter() - t0
     feat.free()
     targ.free()
-    ke_plain, plain_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every)
+    ke_plain, plain_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every,
+                                           tuning=args.tuning)
     with ClockSampler(local) as clk:
-        ke_learn, learn_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every, mlp=net)
+        ke_learn, learn_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every, mlp=net,
+                                               tuning=args.tuning)
     net.close()
     e_plain, e_learn = C.ke_error(ke_plain, ke_ref), C.ke_error(ke_learn, ke_ref)
     if rank != 0:

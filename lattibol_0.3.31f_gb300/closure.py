@@ -185,13 +185,14 @@ class FineRun:
         self.lat.close()
 
 
-def coarse_run(nc, U0, Re, steps, sample_every, mlp=None, z_max=200.0, graph_steps=64):
+def coarse_run(nc, U0, Re, steps, sample_every, mlp=None, z_max=200.0, graph_steps=64,
+               tuning=abi.LB_TUNE_DEFAULT):
     """Coarse Taylor-Green run (plain BGK or with the closure): mean KE at
     every sample (step 0 included) and the wall time.  A run that produces
     non-finite values stops there (returned as NaN from then on)."""
     nu = viscosity(nc, U0, Re)
     lat = Lattice(19, nc, nc, nc, tau_inv=np.float32(1 / (0.5 + 3 * nu)),
-                  graph_steps=graph_steps)
+                  graph_steps=graph_steps, tuning=tuning)
     lat.set_flags(np.zeros(nc ** 3, np.uint8))
     rho, ux, uy, uz = tgv_fields(nc, U0)
     lat.init_equilibrium(rho, ux, uy, uz)

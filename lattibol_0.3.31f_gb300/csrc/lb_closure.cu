@@ -324,15 +324,23 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s) {
     if (!ca.legacy_mma) {
-        // SMs x resident blocks, at most 8 per SM (8 x 64 tensor-memory columns)
+        // SMs x resident blocks.  The occupancy query reports one block per SM
+        // for a kernel that allocates tensor memory, so the residency is
+        // computed from the kernel's registers and shared memory, and capped
+        // at 8 blocks (8 x 64 of the SM's 512 tensor-memory columns).
         static int tc_cap = 0;
         if (!tc_cap) {
-            int dev = 0, sms = 1, occ = 1;
+            int dev = 0, sms = 1, smem_sm = 0, thr_sm = 2048;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, d3q19_closure_tc_kernel<false>,
-                                                          D3_BLOCK, 0);
-            tc_cap = sms * std::min(std::max(occ, 1), 512 / TC_COLS);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+            cudaFuncAttributes fa{};
+            cudaFuncGetAttributes(&fa, d3q19_closure_tc_kernel<false>);
+            const int regs = std::max(1, (fa.numRegs + 7) / 8 * 8 * D3_BLOCK);
+            int occ = std::min({65536 / regs, thr_sm / D3_BLOCK,
+                                smem_sm / (int)(fa.sharedSizeBytes + 1024), 512 / TC_COLS});
+            tc_cap = sms * std::max(occ, 1);
         }
         const long nrows = (long)((a.W + D3_BLOCK - 1) / D3_BLOCK) * a.H * a.D;
         const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
