@@ -361,6 +361,24 @@ int lb_case_load_parameters(const char *path, lb_case_params *out);
 int lb_case_load_solids_bmp(const char *path, int *width, int *height, uint8_t *solids,
                             size_t capacity);
 
+/* Triangles of a binary or ASCII STL file, 9 floats each (three vertices);
+ * call with tri = NULL for the count.  capacity is in floats. */
+int lb_stl_read(const char *path, int64_t *ntri, float *tri, size_t capacity);
+/* The solid mask of a closed triangle surface on the GPU (the stand-in for
+ * the reference's cvmlcpp voxelisation in Input::loadSolidsSTL,
+ * src/input.cpp:118-142, which is not part of the reference tree): the
+ * longest bounding-box side spans max_dim voxels, each axis
+ * ceil(extent / voxel) voxels (dims = W, H, D); a voxel is solid when its
+ * centre is inside the surface (crossing parity along z, fixed-point edge
+ * functions with a consistent tie rule).  solids = NULL: dims only.
+ * *open_columns (may be NULL) is set to 1 when some column crossed the
+ * surface an odd number of times (an open surface). */
+int lb_voxelize(const float *tri, int64_t ntri, int max_dim, int dims[3], uint8_t *solids,
+                size_t capacity, int *open_columns);
+/* lb_stl_read + lb_voxelize: Input::loadSolidsSTL of a 3-D case */
+int lb_case_load_solids_stl(const char *path, int max_dim, int *width, int *height, int *depth,
+                            uint8_t *solids, size_t capacity);
+
 /* The initial D2Q9 state of reference src/simulation_d2q9.cu:100-334 for one
  * device over the whole width, in host memory: f is 9 arrays of
  * width*height floats (f[k*N + node]), the other outputs N values each

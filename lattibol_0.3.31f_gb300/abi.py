@@ -181,6 +181,11 @@ PROTOTYPES = [
     ("lb_case_load_parameters", _c.c_int, [_c.c_char_p, _c.POINTER(lb_case_params)]),
     ("lb_case_load_solids_bmp", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_int),
                                            _c.POINTER(_c.c_int), _c.c_void_p, _c.c_size_t]),
+    ("lb_stl_read", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_int64), _c.c_void_p, _c.c_size_t]),
+    ("lb_voxelize", _c.c_int, [_c.c_void_p, _c.c_int64, _c.c_int, _c.POINTER(_c.c_int),
+                               _c.c_void_p, _c.c_size_t, _c.POINTER(_c.c_int)]),
+    ("lb_case_load_solids_stl", _c.c_int, [_c.c_char_p, _c.c_int] + [_c.POINTER(_c.c_int)] * 3
+     + [_c.c_void_p, _c.c_size_t]),
     ("lb_case_init_d2q9", _c.c_int, [_c.POINTER(lb_case_params), _c.c_int, _c.c_int]
      + [_c.c_void_p] * 9),
     ("lb_case_init_d3q19", _c.c_int, [_c.POINTER(lb_case_params), _c.c_int, _c.c_int, _c.c_int]

@@ -72,10 +72,31 @@ class Input:
         self.solids = mask.reshape(1, h.value, w.value)
         return True
 
+    def loadSolidsSTL(self, fileName):
+        """reference src/input.cpp:118-142: the solids of a 3-D case, voxelised
+        on the GPU at maxDim voxels along the longest side (lb_voxelize)."""
+        L = _lib()
+        n = ctypes.c_int64()
+        rc = L.lb_stl_read(_bytes(fileName), ctypes.byref(n), None, 0)
+        if rc == abi.LB_ERR_IO:
+            return False
+        _check(rc, "lb_stl_read")
+        tri = np.zeros(9 * n.value, np.float32)
+        _check(L.lb_stl_read(_bytes(fileName), ctypes.byref(n), _ptr(tri), tri.size),
+               "lb_stl_read")
+        dims = (ctypes.c_int * 3)()
+        _check(L.lb_voxelize(_ptr(tri), n.value, self.getMaxDim(), dims, None, 0, None),
+               "lb_voxelize")
+        mask = np.zeros(dims[0] * dims[1] * dims[2], np.uint8)
+        _check(L.lb_voxelize(_ptr(tri), n.value, self.getMaxDim(), dims, _ptr(mask), mask.nbytes,
+                             None), "lb_voxelize")
+        self.width, self.height, self.depth = dims[0], dims[1], dims[2]
+        self.solids = mask.reshape(dims[2], dims[1], dims[0])
+        return True
+
     def setSolids(self, solids):
         """A solid mask from the caller: (height, width) or (depth, height,
-        width) -- the stand-in for the reference's STL voxelisation
-        (src/input.cpp:118-142), which needs a library absent here."""
+        width)."""
         s = np.asarray(solids, np.uint8)
         if s.ndim == 2:
             s = s[None]
@@ -88,8 +109,10 @@ class Input:
         if not self.loadParameters(fileName):
             raise LBError("cannot read file %s" % fileName)
         if self.getMaxDim() > 1:
-            raise LBError("3-D cases take their solids from an .stl file: voxelise it and "
-                          "pass the mask to setSolids()")
+            stl = fileName[:-3] + "stl"
+            if not self.loadSolidsSTL(stl):
+                raise LBError("cannot read file %s" % stl)
+            return self
         bmp = fileName[:-3] + "bmp"
         if not self.loadSolids(bmp):
             raise LBError("cannot read file %s" % bmp)
@@ -304,6 +327,7 @@ class SimulationD3Q19(_Simulation):
 
 
 def load_case(fileName):
-    """Input.loadFile plus the matching simulation (2-D cases)."""
+    """Input.loadFile plus the matching simulation (reference
+    src/mainwindow.cpp:267-268: D3Q19 when the case has depth)."""
     inp = Input().loadFile(fileName)
-    return SimulationD2Q9(inp)
+    return SimulationD3Q19(inp) if inp.getLength() > 1 else SimulationD2Q9(inp)

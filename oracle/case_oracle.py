@@ -374,3 +374,104 @@ def pvti_text(vtk_id, device_count, width, height, length):
                    % (i * width, (i + 1) * width, height - 1, length - 1, vtk_id, i))
     out.append("  </PImageData>\n</VTKFile>\n")
     return "".join(out)
+
+
+# ---------------------------------------------------------------- STL solids
+
+def read_stl(path):
+    """Triangles (n, 3, 3) float32 of a binary or ASCII STL file."""
+    with open(path, "rb") as fh:
+        b = fh.read()
+    ascii_ = True
+    if len(b) >= 84:
+        n = struct.unpack_from("<I", b, 80)[0]
+        ascii_ = b[:5] == b"solid" and 84 + 50 * n != len(b)
+    if ascii_:
+        toks = b.decode("latin-1").split()
+        vals = []
+        for i, t in enumerate(toks):
+            if t == "vertex":
+                vals += [np.float32(float(toks[i + 1])), np.float32(float(toks[i + 2])),
+                         np.float32(float(toks[i + 3]))]
+        return np.array(vals, np.float32).reshape(-1, 3, 3)
+    dt = np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")])
+    return np.frombuffer(b, dt, count=n, offset=84)["v"].astype(np.float32)
+
+
+def voxel_grid(tri, max_dim):
+    """(lo[3], h, dims[3]) of the voxel grid: the longest bounding-box side
+    spans max_dim voxels, each axis ceil(extent / h) voxels."""
+    v = np.asarray(tri, np.float32).reshape(-1, 3).astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    ext = max(hi - lo)
+    h = ext / max_dim
+    dims = [max(1, int(math.ceil((hi[a] - lo[a]) / h - 1e-9))) for a in range(3)]
+    return lo, h, dims
+
+
+def _round_half_away(v):
+    f = np.floor(v)
+    return np.where(v - f >= 0.5, f + 1, f).astype(np.int64)
+
+
+def voxelize(tri, max_dim):
+    """Solid mask (D, H, W) of a closed triangle surface: voxel centres with
+    an odd number of surface crossings below them in their z column, the
+    crossings found with fixed-point (2^-16 voxel) edge functions and a
+    consistent tie rule (the library's lb_voxelize, restated)."""
+    FRAC = 16
+    tri = np.asarray(tri, np.float32).reshape(-1, 3, 3)
+    lo, h, (W, H, D) = voxel_grid(tri, max_dim)
+    sc = float(1 << FRAC) / h
+    q = _round_half_away((tri.astype(np.float64) - lo[None, None, :]) * sc)  # (n, 3 vertices, 3)
+    cols, zs = [], []
+    inv = 1.0 / float(1 << FRAC)
+    for t in range(len(q)):
+        (x0, y0, z0), (x1, y1, z1), (x2, y2, z2) = [tuple(int(c) for c in q[t, v]) for v in range(3)]
+        area = (x1 - x0) * (y2 - y0) - (y1 - y0) * (x2 - x0)
+        if area == 0:
+            continue
+        if area < 0:
+            x1, y1, z1, x2, y2, z2 = x2, y2, z2, x1, y1, z1
+        bx0 = int(math.floor(min(x0, x1, x2) * inv - 0.5))
+        bx1 = int(math.ceil(max(x0, x1, x2) * inv - 0.5))
+        by0 = int(math.floor(min(y0, y1, y2) * inv - 0.5))
+        by1 = int(math.ceil(max(y0, y1, y2) * inv - 0.5))
+        xs = np.arange(max(bx0, 0), min(bx1, W - 1) + 1, dtype=np.int64)
+        ys = np.arange(max(by0, 0), min(by1, H - 1) + 1, dtype=np.int64)
+        if len(xs) == 0 or len(ys) == 0:
+            continue
+        X, Y = np.meshgrid(xs, ys)
+        px = (2 * X + 1) << (FRAC - 1)
+        py = (2 * Y + 1) << (FRAC - 1)
+
+        def ef(ax, ay, bx, by):
+            e = (bx - ax) * (py - ay) - (by - ay) * (px - ax)
+            dx, dy = bx - ax, by - ay
+            tie = (dy > 0) or (dy == 0 and dx < 0)
+            return e, (e > 0) | ((e == 0) & tie)
+
+        e0, k0 = ef(x1, y1, x2, y2)
+        e1, k1 = ef(x2, y2, x0, y0)
+        e2, k2 = ef(x0, y0, x1, y1)
+        m = k0 & k1 & k2
+        if not m.any():
+            continue
+        e0, e1, e2 = (e[m].astype(np.float64) for e in (e0, e1, e2))
+        a = e0 + e1 + e2
+        z = (e0 * float(z0) + e1 * float(z1) + e2 * float(z2)) / a
+        cols.append((Y[m] * W + X[m]).astype(np.int64))
+        zs.append(z)
+    solid = np.zeros((D, H * W), np.uint8)
+    if cols:
+        c = np.concatenate(cols)
+        z = np.concatenate(zs)
+        order = np.lexsort((z, c))
+        c, z = c[order], z[order]
+        centres = np.array([float((2 * k + 1) << (FRAC - 1)) for k in range(D)])
+        starts = np.flatnonzero(np.r_[True, c[1:] != c[:-1]])
+        ends = np.r_[starts[1:], len(c)]
+        for s, e in zip(starts, ends):
+            below = np.searchsorted(z[s:e], centres, side="left")
+            solid[:, c[s]] = (below & 1).astype(np.uint8)
+    return solid.reshape(D, H, W)

@@ -6,8 +6,10 @@ Run from the repository root where the reference tree exists:
     python tests/golden/make_case_fixtures.py [reference root]
 
 cases.json holds, per case, the parsed parameters (floats as IEEE-754 bit
-patterns) and, for 2-D cases, the mask's size, solid count and SHA-256;
-case_masks.npz holds each distinct mask bit-packed.  The tests need neither
+patterns) and, for 2-D cases, the mask's size, solid count and SHA-256; for
+3-D cases the voxelisation of the STL surface at the case's max_dim (size,
+solid count, SHA-256).  case_masks.npz holds each distinct 2-D mask
+bit-packed, case_stl.npz each distinct STL surface as float32 triangles.  The tests need neither
 the reference nor this script.
 """
 import hashlib
@@ -42,7 +44,7 @@ def params_json(p):
 
 def main(ref_root):
     samples = os.path.join(ref_root, "samples")
-    cases, masks = [], {}
+    cases, masks, triangles = [], {}, {}
     for dirpath, _dirs, files in sorted(os.walk(samples)):
         for fn in sorted(files):
             if not fn.endswith(".dat"):
@@ -52,6 +54,15 @@ def main(ref_root):
             p = case_oracle.load_parameters(dat)
             entry = {"name": rel, "params": params_json(p)}
             bmp = dat[:-3] + "bmp"
+            stl = dat[:-3] + "stl"
+            if p["max_dim"] > 1 and os.path.exists(stl):
+                tri = case_oracle.read_stl(stl)
+                key = "t_" + hashlib.sha256(tri.tobytes()).hexdigest()[:16]
+                triangles[key] = tri
+                mask = case_oracle.voxelize(tri, p["max_dim"])
+                entry.update(stl=key, stl_dims=list(mask.shape[::-1]),
+                             stl_solids=int(mask.sum()),
+                             stl_sha256=hashlib.sha256(mask.tobytes()).hexdigest())
             if p["max_dim"] <= 1 and os.path.exists(bmp):
                 w, h, mask = case_oracle.load_solids_bmp(bmp)
                 sha = hashlib.sha256(mask.tobytes()).hexdigest()
@@ -62,7 +73,9 @@ def main(ref_root):
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1)
     np.savez_compressed(os.path.join(HERE, "case_masks.npz"), **masks)
-    print("%d cases, %d distinct masks" % (len(cases), len(masks)))
+    np.savez_compressed(os.path.join(HERE, "case_stl.npz"), **triangles)
+    print("%d cases, %d distinct masks, %d distinct STL surfaces"
+          % (len(cases), len(masks), len(triangles)))
 
 
 if __name__ == "__main__":

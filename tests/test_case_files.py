@@ -467,3 +467,102 @@ def test_checkpoint_info_rejects_non_checkpoints(pkg, tmp_path):
     assert L.lb_checkpoint_info(os.fsencode(tmp_path / "none"), ctypes.byref(cfg),
                                 ctypes.byref(steps)) == pkg.abi.LB_ERR_IO
     L.lb_abi_clear_error()
+
+
+# ------------------------------------------------------------------ STL files
+
+def stl_fixtures():
+    return np.load(os.path.join(GOLDEN, "case_stl.npz"))
+
+
+def lib_read_stl(pkg, path):
+    L = lib(pkg)
+    n = ctypes.c_int64()
+    assert L.lb_stl_read(os.fsencode(path), ctypes.byref(n), None, 0) == 0
+    tri = np.zeros(9 * n.value, np.float32)
+    assert L.lb_stl_read(os.fsencode(path), ctypes.byref(n),
+                         tri.ctypes.data_as(ctypes.c_void_p), tri.size) == 0
+    return tri.reshape(-1, 3, 3)
+
+
+def write_binary_stl(path, tri, header=b"binary"):
+    tri = np.asarray(tri, np.float32).reshape(-1, 3, 3)
+    rec = np.zeros(len(tri), np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]))
+    rec["v"] = tri
+    path.write_bytes(header.ljust(80, b" ") + struct.pack("<I", len(tri)) + rec.tobytes())
+
+
+def write_ascii_stl(path, tri):
+    lines = ["solid test"]
+    for t in np.asarray(tri, np.float32).reshape(-1, 3, 3):
+        lines += ["  facet normal 0 0 0", "    outer loop"]
+        lines += ["      vertex %.9g %.9g %.9g" % tuple(float(c) for c in v) for v in t]
+        lines += ["    endloop", "  endfacet"]
+    path.write_text("\n".join(lines + ["endsolid test", ""]))
+
+
+def test_stl_reader_binary_ascii_and_solid_header(pkg, tmp_path):
+    rng = np.random.default_rng(2)
+    tri = rng.standard_normal((37, 3, 3)).astype(np.float32) * 10
+    write_binary_stl(tmp_path / "b.stl", tri)
+    write_binary_stl(tmp_path / "s.stl", tri, header=b"solid but binary")
+    write_ascii_stl(tmp_path / "a.stl", tri)
+    for name in ("b.stl", "s.stl", "a.stl"):
+        got = lib_read_stl(pkg, tmp_path / name)
+        assert np.array_equal(got, co.read_stl(str(tmp_path / name))), name
+        assert np.array_equal(got, tri), name
+    n = ctypes.c_int64()
+    assert lib(pkg).lb_stl_read(os.fsencode(tmp_path / "none.stl"), ctypes.byref(n), None, 0) \
+        == pkg.abi.LB_ERR_IO
+    lib(pkg).lb_abi_clear_error()
+
+
+@pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference samples not present")
+def test_library_reads_every_sample_stl_like_the_fixtures(pkg):
+    cases, _ = fixtures()
+    surf = stl_fixtures()
+    for e in cases:
+        if "stl" in e:
+            got = lib_read_stl(pkg, os.path.join(SAMPLES, e["name"][:-3] + "stl"))
+            assert np.array_equal(got, surf[e["stl"]]), e["name"]
+
+
+def test_voxel_grid_dims_vs_oracle(pkg):
+    """lb_voxelize with no output buffer computes the grid on the host."""
+    cases, _ = fixtures()
+    surf = stl_fixtures()
+    n3d = 0
+    for e in cases:
+        if "stl" not in e:
+            continue
+        tri = np.ascontiguousarray(surf[e["stl"]], np.float32)
+        dims = (ctypes.c_int * 3)()
+        assert lib(pkg).lb_voxelize(tri.ctypes.data_as(ctypes.c_void_p), len(tri),
+                                    e["params"]["max_dim"], dims, None, 0, None) == 0
+        _, _, want = co.voxel_grid(tri, e["params"]["max_dim"])
+        assert list(dims) == want == e["stl_dims"], e["name"]
+        n3d += 1
+    assert n3d >= 6
+
+
+def test_oracle_voxeliser_on_closed_shapes():
+    """The oracle voxeliser on shapes whose solid voxels are known: an
+    axis-aligned box, and a box with a box-shaped hole (two closed surfaces),
+    faces between voxel centres."""
+    def box(lo, hi):
+        x0, y0, z0 = lo
+        x1, y1, z1 = hi
+        v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                      [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float32)
+        f = [(0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4),
+             (2, 3, 7), (2, 7, 6), (1, 2, 6), (1, 6, 5), (3, 0, 4), (3, 4, 7)]
+        return v[np.array(f)]
+    # the bounding box is the box itself: 20 x 10 x 6 units, max_dim 20 -> 1 unit voxels
+    m = co.voxelize(box((0, 0, 0), (20, 10, 6)), 20)
+    assert m.shape == (6, 10, 20) and m.all()
+    # a box inside a larger frame box (two closed surfaces): the inner one is a hole
+    tri = np.concatenate([box((0, 0, 0), (20, 10, 6)), box((5, 2, 1), (15, 8, 5))])
+    m = co.voxelize(tri, 20)
+    hole = np.zeros((6, 10, 20), bool)
+    hole[1:5, 2:8, 5:15] = True
+    assert np.array_equal(m.astype(bool), ~hole)

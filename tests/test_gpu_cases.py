@@ -1,5 +1,6 @@
 """GPU: the reference's sample cases run headless through the drop-in entry
-points (Input -> SimulationD2Q9 -> runLBM), bit-exact against the oracle;
+points (Input -> SimulationD2Q9/D3Q19 -> runLBM; 3-D solids voxelised from
+the cases' STL surfaces on the GPU), bit-exact against the oracle;
 checkpoint/resume bit-identity; VTK output of a context."""
 import json
 import os
@@ -212,3 +213,106 @@ def test_context_vtk_matches_oracle(pkg, tmp_path):
     text = (tmp_path / "r0007p00.vti").read_text()
     assert text == co.vtk_text(0, kw["nx"], kw["ny"], kw["nz"], r, ux, uy, uz)
     lat.close()
+
+
+# ----------------------------------------------------------------- 3-D cases
+
+def gpu_voxelize(pkg, tri, max_dim):
+    import ctypes
+    L = pkg.lib()
+    tri = np.ascontiguousarray(tri, np.float32)
+    P = tri.ctypes.data_as(ctypes.c_void_p)
+    dims = (ctypes.c_int * 3)()
+    assert L.lb_voxelize(P, len(tri), max_dim, dims, None, 0, None) == 0
+    W, H, D = dims
+    m = np.zeros(W * H * D, np.uint8)
+    opn = ctypes.c_int(-1)
+    assert L.lb_voxelize(P, len(tri), max_dim, dims, m.ctypes.data_as(ctypes.c_void_p),
+                         m.nbytes, ctypes.byref(opn)) == 0, L.lb_abi_last_error()
+    return m.reshape(D, H, W), opn.value
+
+
+def box(lo, hi):
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float32)
+    f = [(0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4),
+         (2, 3, 7), (2, 7, 6), (1, 2, 6), (1, 6, 5), (3, 0, 4), (3, 4, 7)]
+    return v[np.array(f)]
+
+
+def test_voxelize_boxes_and_random_surfaces_vs_oracle(pkg):
+    m, opn = gpu_voxelize(pkg, box((0, 0, 0), (20, 10, 6)), 20)
+    assert m.shape == (6, 10, 20) and m.all() and opn == 0
+    # a hole whose faces pass through voxel centres, and a rotated box: the
+    # tie rule and the fixed-point depths must give the oracle's voxels
+    rng = np.random.default_rng(12)
+    rot = np.linalg.qr(rng.standard_normal((3, 3)))[0].astype(np.float32)
+    shapes = [np.concatenate([box((0, 0, 0), (20, 10, 6)), box((5.5, 2.5, 1.5), (14.5, 7.5, 4.5))]),
+              (box((-3, -2, -1), (3, 2, 1)) @ rot.T).astype(np.float32)]
+    for tri, md in zip(shapes, (20, 48)):
+        m, opn = gpu_voxelize(pkg, tri, md)
+        assert opn == 0
+        assert np.array_equal(m, co.voxelize(tri, md))
+
+
+def test_voxelize_sample_surfaces_like_the_fixtures(pkg):
+    import hashlib
+    cases, _ = fixtures()
+    surf = np.load(os.path.join(os.path.dirname(__file__), "golden", "case_stl.npz"))
+    n = 0
+    for e in cases:
+        if "stl" not in e:
+            continue
+        m, _ = gpu_voxelize(pkg, surf[e["stl"]], e["params"]["max_dim"])
+        assert list(m.shape[::-1]) == e["stl_dims"], e["name"]
+        assert hashlib.sha256(m.tobytes()).hexdigest() == e["stl_sha256"], e["name"]
+        n += 1
+    assert n >= 6
+
+
+STEPS3 = 8
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["standalone", "fused"])
+def test_3d_sample_cases_vs_oracle(pkg, oracle, mode):
+    """The reference's 3-D sample cases (the .dat parameters, the STL surface
+    voxelised on the GPU) for 8 steps of SimulationD3Q19.runLBM through the
+    drop-in, bit-exact against the oracle from the same initial state."""
+    cases, _ = fixtures()
+    surf = np.load(os.path.join(os.path.dirname(__file__), "golden", "case_stl.npz"))
+    L = pkg.lib()
+    seen = set()
+    assert L.lb_abi_set_mode(mode) == 0
+    try:
+        for e in cases:
+            if "stl" not in e:
+                continue
+            key = (e["stl"], json.dumps(e["params"], sort_keys=True))
+            if key in seen:
+                continue
+            seen.add(key)
+            p = fixture_params(e)
+            mask, _ = gpu_voxelize(pkg, surf[e["stl"]], p["max_dim"])
+            D, H, W = mask.shape
+            sim = pkg.SimulationD3Q19(make_input(pkg, p, mask))
+            sim.runLBM(STEPS3)
+            init = co.init_d3q19(p, mask)
+            f = init["f"].copy()
+            mom = [init[k].copy() for k in ("ux", "uy", "uz", "rho")]
+            solid = np.ascontiguousarray(mask.reshape(-1), np.uint8)
+            plot = np.zeros(4 * W * H * D, np.float32)
+            for _ in range(STEPS3):
+                oracle.d3q19_stream(f, init["solid_bound"], W, H, D)
+                oracle.d3q19_collide(f, solid, mom, W, H, D, *pkg.W3, p["tau_inv"], p["ux"],
+                                     p["uy"], p["uz"], p["rho"], plot=plot)
+            assert L.lb_abi_release_d3q19(sim.data.ptr()) == 0
+            assert beq(sim.populations(), f), e["name"]
+            for k, a in zip(("ux", "uy", "uz", "rho"), mom):
+                assert beq(sim.field(k), a), (e["name"], k)
+            assert beq(sim.data.plot_data(), plot), e["name"]
+            sim.close()
+        assert len(seen) >= 6
+    finally:
+        L.lb_abi_set_mode(0)
