@@ -4,8 +4,8 @@
 // All domains live in one packed structure-of-arrays slab (domain d occupies
 // nodes [off_d, off_d + W_d*H_d), node x + W_d*y inside it), in two
 // population sets that alternate like the single-lattice context.  A step is
-// two persistent launches over a host-built work list of row groups
-// (domain, first row): the density pass writes psi = psi(rho) of every node,
+// two persistent launches over a host-built work list of row groups (a
+// domain's extents and physics and a first row): the density pass writes psi = psi(rho) of every node,
 // the fused pass pulls the populations, adds the Shan-Chen shift from the
 // 3x3 psi stencil and relaxes.  Each block walks the work list with a stride
 // of the grid size, and the grid is a multiple of the SM count, so uneven
@@ -34,20 +34,27 @@ struct EnsDomain {
     float G, tau_inv;
 };
 
+// one work item: a group of rows of one domain, with the domain's extents
+// and physics copied in, so that a block needs one load (not two dependent
+// ones) before it can address its populations
+struct EnsItem {
+    int off, W, H, y;
+    float G, tau_inv;
+};
+
 struct EnsArgs {
     const float *src[9];
     float *dst[9];
     float *psi;
     float *rho, *ux, *uy;
-    const EnsDomain *dom;
-    const int2 *items;  // (domain, first row)
+    const EnsItem *items;
     int nitems;
     int psi_form;
     float w0, w1, w5;
 };
 
 // pull of node (x, y) of a periodic domain starting at node `off`
-__device__ __forceinline__ void ens_pull(const EnsArgs &a, const EnsDomain &dm, int x, int y,
+__device__ __forceinline__ void ens_pull(const EnsArgs &a, const EnsItem &dm, int x, int y,
                                          float (&g)[9]) {
     const int xm = x == 0 ? dm.W - 1 : x - 1, xp = x == dm.W - 1 ? 0 : x + 1;
     const int rm = y == 0 ? dm.H - 1 : y - 1, rp = y == dm.H - 1 ? 0 : y + 1;
@@ -60,28 +67,39 @@ __device__ __forceinline__ void ens_pull(const EnsArgs &a, const EnsDomain &dm, 
     }
 }
 
+// Both passes walk the work list with a stride of the grid size and load the
+// next item while they work on the current one.
 __global__ void ens_density_kernel(const EnsArgs a) {
-    for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
-        const int2 item = a.items[it];
-        const EnsDomain dm = a.dom[item.x];
-        const int y = item.y + threadIdx.y;
-        if (y >= dm.H) continue;
-        for (int x = threadIdx.x; x < dm.W; x += blockDim.x) {
-            float g[9];
-            ens_pull(a, dm, x, y, g);
-            float rho, ux, uy;
-            d2q9_moments(g, rho, ux, uy);
-            a.psi[dm.off + x + dm.W * y] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+    int it = blockIdx.x;
+    if (it >= a.nitems) return;
+    EnsItem dm = a.items[it];
+    for (; it < a.nitems; it += gridDim.x) {
+        const int nit = it + gridDim.x;
+        const EnsItem next = nit < a.nitems ? a.items[nit] : dm;
+        const int y = dm.y + threadIdx.y;
+        if (y < dm.H) {
+            for (int x = threadIdx.x; x < dm.W; x += blockDim.x) {
+                float g[9];
+                ens_pull(a, dm, x, y, g);
+                float rho, ux, uy;
+                d2q9_moments(g, rho, ux, uy);
+                a.psi[dm.off + x + dm.W * y] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+            }
         }
+        dm = next;
     }
 }
 
 template <bool MOM>
 __global__ void ens_fused_kernel(const EnsArgs a) {
-    for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
-        const int2 item = a.items[it];
-        const EnsDomain dm = a.dom[item.x];
-        const int y = item.y + threadIdx.y;
+    int it = blockIdx.x;
+    if (it >= a.nitems) return;
+    EnsItem next = a.items[it];
+    for (; it < a.nitems; it += gridDim.x) {
+        const EnsItem dm = next;
+        const int nit = it + gridDim.x;
+        if (nit < a.nitems) next = a.items[nit];
+        const int y = dm.y + threadIdx.y;
         if (y >= dm.H) continue;
         const int rm = y == 0 ? dm.H - 1 : y - 1, rp = y == dm.H - 1 ? 0 : y + 1;
         const float *psi = a.psi + dm.off;
@@ -118,10 +136,9 @@ struct lb_ensemble {
     int nd = 0;
     std::vector<EnsDomain> dom;
     long NT = 0, stride = 0;
-    EnsDomain *dom_d = nullptr;
     float *pop[2] = {nullptr, nullptr};
     float *psi = nullptr, *mom = nullptr;
-    int2 *items_d = nullptr;
+    EnsItem *items_d = nullptr;
     int nitems = 0, items_cap = 0;
     int cur = 0, psi_form = LB_PSI_EXP1, sms = 1, graph_steps = 32;
     LaunchShape shape{128, 1, 4};
@@ -157,7 +174,6 @@ EnsArgs args_for(lb_ensemble *e, int from) {
     }
     a.psi = e->psi;
     a.rho = e->mom; a.ux = e->mom + e->stride; a.uy = e->mom + 2 * e->stride;
-    a.dom = e->dom_d;
     a.items = e->items_d;
     a.nitems = e->nitems;
     a.psi_form = e->psi_form;
@@ -188,16 +204,19 @@ void drop_graphs(lb_ensemble *e) {
 
 // work list of row groups for the current shape
 int build_items(lb_ensemble *e) {
-    std::vector<int2> items;
+    std::vector<EnsItem> items;
     for (int d = 0; d < e->nd; d++)
-        for (int y = 0; y < e->dom[d].H; y += e->shape.ry) items.push_back(make_int2(d, y));
+        for (int y = 0; y < e->dom[d].H; y += e->shape.ry) {
+            const EnsDomain &m = e->dom[d];
+            items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv});
+        }
     if ((int)items.size() > e->items_cap) {
         if (e->items_d) cudaFree(e->items_d);
         e->items_d = nullptr;
-        LB_ETRY(e, "work list", cudaMalloc(&e->items_d, sizeof(int2) * items.size()));
+        LB_ETRY(e, "work list", cudaMalloc(&e->items_d, sizeof(EnsItem) * items.size()));
         e->items_cap = (int)items.size();
     }
-    LB_ETRY(e, "work list", cudaMemcpy(e->items_d, items.data(), sizeof(int2) * items.size(),
+    LB_ETRY(e, "work list", cudaMemcpy(e->items_d, items.data(), sizeof(EnsItem) * items.size(),
                                        cudaMemcpyHostToDevice));
     e->nitems = (int)items.size();
     drop_graphs(e);
@@ -254,9 +273,6 @@ int lb_ensemble_create(int nd, const int *nx, const int *ny, const float *G, con
     if (c == cudaSuccess) c = cudaMalloc(&e->pop[1], sizeof(float) * 9 * e->stride);
     if (c == cudaSuccess) c = cudaMalloc(&e->psi, sizeof(float) * e->stride);
     if (c == cudaSuccess) c = cudaMalloc(&e->mom, sizeof(float) * 3 * e->stride);
-    if (c == cudaSuccess) c = cudaMalloc(&e->dom_d, sizeof(EnsDomain) * nd);
-    if (c == cudaSuccess)
-        c = cudaMemcpy(e->dom_d, e->dom.data(), sizeof(EnsDomain) * nd, cudaMemcpyHostToDevice);
     if (c == cudaSuccess) c = cudaMemset(e->mom, 0, sizeof(float) * 3 * e->stride);
     if (c == cudaSuccess) c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (c == cudaSuccess) c = cudaEventCreate(&e->ev0);
@@ -281,7 +297,6 @@ int lb_ensemble_destroy(lb_ensemble *e) {
         if (e->pop[i]) cudaFree(e->pop[i]);
     if (e->psi) cudaFree(e->psi);
     if (e->mom) cudaFree(e->mom);
-    if (e->dom_d) cudaFree(e->dom_d);
     if (e->items_d) cudaFree(e->items_d);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
