@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
         if (fluid) {
             const Nbr3 n(x, y, z, a.W, a.H, a.D);
             pull_native<float>(a, o, n, fl, g);
-            d3q19_moments(g, rho, ux, uy, uz);
+            d3q19_moments_native(g, rho, ux, uy, uz);
             closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
         }
         __nv_bfloat162 *row = reinterpret_cast<__nv_bfloat162 *>(sw.x + lane * SX_STRIDE);
@@ -126,10 +126,13 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
         if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
         if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
         float ex = ux, ey = uy, ez = uz;
-        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
-        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
-        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
-        d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+        if (a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
+            const float inv_rt = 1.f / (rho * tau_inv);
+            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+        }
+        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
 #pragma unroll
         for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
     }
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         if (fluid) {
             const Nbr3 n(x, y, z, a.W, a.H, a.D);
             pull_native<float>(a, o, n, fl, g);
-            d3q19_moments(g, rho, ux, uy, uz);
+            d3q19_moments_native(g, rho, ux, uy, uz);
             closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
         }
         // 1. features -> row t of A (four 16-byte column groups, K = 32)
@@ -302,10 +305,13 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
         if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
         float ex = ux, ey = uy, ez = uz;
-        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * tau_inv);
-        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * tau_inv);
-        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * tau_inv);
-        d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+        if (a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
+            const float inv_rt = 1.f / (rho * tau_inv);
+            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+        }
+        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
 #pragma unroll
         for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
     }

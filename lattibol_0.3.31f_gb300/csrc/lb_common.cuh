@@ -153,6 +153,81 @@ __device__ __forceinline__ void d3q19_moments(const float (&g)[19], float &rho, 
     uz = (g[5] + g[9] + g[13] + g[15] + g[17] - g[6] - g[10] - g[14] - g[16] - g[18]) / rho;
 }
 
+// ------------------------------------------------ native-mode D3Q19 arithmetic
+// The native mode (no reference counterpart) is free to associate its
+// arithmetic for fewer instructions; the oracle restates the same order and
+// the same fused multiply-adds (fmaf), so the results stay bit-identical.
+
+// density as the sum of the cx = +1, -1 and 0 partial sums (shared with j_x)
+__device__ __forceinline__ void d3q19_xsums_native(const float (&g)[19], float &px, float &mx,
+                                                   float &zx) {
+    px = (g[1] + g[7]) + (g[8] + g[9]) + g[10];
+    mx = (g[2] + g[11]) + (g[12] + g[13]) + g[14];
+    zx = ((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17])) + g[18];
+}
+__device__ __forceinline__ float d3q19_rho_native(const float (&g)[19]) {
+    float px, mx, zx;
+    d3q19_xsums_native(g, px, mx, zx);
+    return (px + mx) + zx;
+}
+
+// density and bare velocity: one division gives 1/rho
+__device__ __forceinline__ void d3q19_moments_native(const float (&g)[19], float &rho,
+                                                     float &ux, float &uy, float &uz) {
+    float px, mx, zx;
+    d3q19_xsums_native(g, px, mx, zx);
+    rho = (px + mx) + zx;
+    const float jy = ((g[3] + g[7]) + (g[11] + g[15]) + g[16]) -
+                     ((g[4] + g[8]) + (g[12] + g[17]) + g[18]);
+    const float jz = ((g[5] + g[9]) + (g[13] + g[15]) + g[17]) -
+                     ((g[6] + g[10]) + (g[14] + g[16]) + g[18]);
+    const float inv = 1.f / rho;
+    ux = (px - mx) * inv;
+    uy = jy * inv;
+    uz = jz * inv;
+}
+
+// BGK at velocity (ux, uy, uz): per opposite pair with projection p,
+// t = 1 - 1.5 u^2 + 4.5 p^2 once, f_eq = w rho (t +- 3 p), f += tau_inv (f_eq - f)
+__device__ __forceinline__ void d3q19_bgk_native(float (&g)[19], float ux, float uy, float uz,
+                                                 float rho, float w0, float w1, float w7,
+                                                 float tau_inv) {
+    const float usq = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, ux * ux));
+    const float base = __fmaf_rn(-1.5f, usq, 1.f);
+    const float a0 = w0 * rho, a1 = w1 * rho, a7 = w7 * rho;
+    g[0] = __fmaf_rn(tau_inv, a0 * base - g[0], g[0]);
+    auto pair = [&](int kp, int km, float a, float p) {
+        const float t = __fmaf_rn(4.5f * p, p, base);
+        const float fp = a * __fmaf_rn(3.f, p, t), fm = a * __fmaf_rn(-3.f, p, t);
+        g[kp] = __fmaf_rn(tau_inv, fp - g[kp], g[kp]);
+        g[km] = __fmaf_rn(tau_inv, fm - g[km], g[km]);
+    };
+    pair(1, 2, a1, ux);
+    pair(3, 4, a1, uy);
+    pair(5, 6, a1, uz);
+    pair(7, 12, a7, ux + uy);
+    pair(8, 11, a7, ux - uy);
+    pair(9, 14, a7, ux + uz);
+    pair(10, 13, a7, ux - uz);
+    pair(15, 18, a7, uy + uz);
+    pair(16, 17, a7, uy - uz);
+}
+
+// Shan-Chen interaction sum over the 18 neighbours, ps[k] = psi(x + c_k):
+// IF = sum_k w_k psi(x + c_k) c_k, grouped by the sign of each component
+__device__ __forceinline__ void d3q19_sc_sum_native(const float (&ps)[19], float w1, float w7,
+                                                    float &IFx, float &IFy, float &IFz) {
+    IFx = __fmaf_rn(w1, ps[1] - ps[2],
+                    w7 * (((ps[7] + ps[8]) + (ps[9] + ps[10])) -
+                          ((ps[11] + ps[12]) + (ps[13] + ps[14]))));
+    IFy = __fmaf_rn(w1, ps[3] - ps[4],
+                    w7 * (((ps[7] + ps[11]) + (ps[15] + ps[16])) -
+                          ((ps[8] + ps[12]) + (ps[17] + ps[18]))));
+    IFz = __fmaf_rn(w1, ps[5] - ps[6],
+                    w7 * (((ps[9] + ps[13]) + (ps[15] + ps[17])) -
+                          ((ps[10] + ps[14]) + (ps[16] + ps[18]))));
+}
+
 // Zou-He velocity inlet at the west face, reference src/collision.cu:412-430
 // (the reference's double literals promote these lines to FP64)
 __device__ __forceinline__ void d3q19_zou_he_west(float (&g)[19], float ux_in) {

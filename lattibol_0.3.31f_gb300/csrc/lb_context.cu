@@ -124,14 +124,9 @@ bool persistent_on(const lb_ctx *c) {
     return c->Q == 9 && !sc_on(c) && (c->tune & LB_TUNE_PERSISTENT);
 }
 
-// the step kernels write the cursor probe themselves on every path except the
-// single-pass Shan-Chen kernel
-bool probe_in_step(const lb_ctx *c) {
-    if (c->Q == 9) return true;
-    if (c->closure_on) return true;
-    return !(c->cfg.mode == LB_MODE_NATIVE && sc_on(c) && (c->tune & LB_TUNE_SC_SINGLE_PASS) &&
-             sc_march_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz));
-}
+// the step kernels write the cursor probe themselves (every step path does;
+// the per-step fallback in lb_run_probe stays for paths that might not)
+bool probe_in_step(const lb_ctx *) { return true; }
 
 // forget the captured step graphs (their kernel arguments changed)
 void drop_graphs(lb_ctx *c) {

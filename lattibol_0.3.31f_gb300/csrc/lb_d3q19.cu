@@ -77,41 +77,46 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
             d3q19_zou_he_east(g, a.rho_out);
     }
     float rho, ux, uy, uz;
-    d3q19_moments(g, rho, ux, uy, uz);
+    if (MODE == MODE_NATIVE) d3q19_moments_native(g, rho, ux, uy, uz);
+    else d3q19_moments(g, rho, ux, uy, uz);
     if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
     if (PLOT) a.plot[o] = make_float4(ux, uy, uz, rho);
     if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
-    float ex = ux, ey = uy, ez = uz;
     if (MODE == MODE_NATIVE) {
-        // velocity-shift forcing, the form of reference src/collision.cu:280-284
-        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
-        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
-        if (a.Fz != 0.f) ez = uz + a.Fz / (rho * a.tau_inv);
-        if (SC) {
-            float IFx = 0.f, IFy = 0.f, IFz = 0.f;
+        float ex = ux, ey = uy, ez = uz;
+        // velocity-shift forcing (the form of reference src/collision.cu:280-284)
+        // and the Shan-Chen shift share one division, 1 / (rho tau_inv)
+        if (SC || a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
+            const float inv_rt = 1.f / (rho * a.tau_inv);
+            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+            if (SC) {
+                float ps[19];
+                ps[0] = a.psi[o];
 #pragma unroll
-            for (int k = 1; k < 19; k++) {
-                const float t = (k < 7 ? a.w1 : a.w7) *
-                                __ldg(a.psi + o + n.off(d3_cx(k), d3_cy(k), d3_cz(k)));
-                if (d3_cx(k) > 0) IFx = IFx + t; else if (d3_cx(k) < 0) IFx = IFx - t;
-                if (d3_cy(k) > 0) IFy = IFy + t; else if (d3_cy(k) < 0) IFy = IFy - t;
-                if (d3_cz(k) > 0) IFz = IFz + t; else if (d3_cz(k) < 0) IFz = IFz - t;
+                for (int k = 1; k < 19; k++)
+                    ps[k] = __ldg(a.psi + o + n.off(d3_cx(k), d3_cy(k), d3_cz(k)));
+                float IFx, IFy, IFz;
+                d3q19_sc_sum_native(ps, a.w1, a.w7, IFx, IFy, IFz);
+                const float c = (-a.G * ps[0]) * inv_rt;
+                ex = __fmaf_rn(c, IFx, ex);
+                ey = __fmaf_rn(c, IFy, ey);
+                ez = __fmaf_rn(c, IFz, ez);
             }
-            const float gp = -a.G * a.psi[o];
-            ex = ex + (gp * IFx) / (a.tau_inv * rho);
-            ey = ey + (gp * IFy) / (a.tau_inv * rho);
-            ez = ez + (gp * IFz) / (a.tau_inv * rho);
         }
+        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+    } else {
+        d3q19_bgk(g, ux, uy, uz, rho, a.w0, a.w1, a.w7, a.tau_inv);
     }
-    d3q19_bgk(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
     S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
     for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], a.wr[k]);
 }
 
 // Density pass of the Shan-Chen step: psi(rho) of the post-stream density of
-// every fluid node (the sum in the order of the collision's moments, so rho
-// is the same float the fused kernel computes), 0 at walls.
+// every fluid node (the native moments' sum, so rho is the same float the
+// fused kernel computes), 0 at walls.
 template <typename S>
 __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a) {
     const Coord3 c(a);
@@ -125,8 +130,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a)
     const Nbr3 n(c.x, c.y, c.z, a.W, a.H, a.D);
     float g[19];
     pull_native<S>(a, o, n, fl, g);
-    const float rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8] + g[9] +
-                      g[10] + g[11] + g[12] + g[13] + g[14] + g[15] + g[16] + g[17] + g[18];
+    const float rho = d3q19_rho_native(g);
     a.psi[o] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
@@ -153,8 +157,7 @@ __device__ __forceinline__ float sc_psi_of_node(const D3Args &a, int x, int y, i
     const Nbr3 n(x, y, zz, a.W, a.H, a.D);
     float g[19];
     pull_native<S>(a, o, n, fl, g);
-    const float rho = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8] + g[9] +
-                      g[10] + g[11] + g[12] + g[13] + g[14] + g[15] + g[16] + g[17] + g[18];
+    const float rho = d3q19_rho_native(g);
     return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
@@ -187,10 +190,7 @@ __global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args
         if (!(fl & CELL_WALL)) {
             const Nbr3 n(x, y, zz, a.W, a.H, a.D);
             pull_native<S>(a, o, n, fl, g_next);
-            const float rho = g_next[0] + g_next[1] + g_next[2] + g_next[3] + g_next[4] +
-                              g_next[5] + g_next[6] + g_next[7] + g_next[8] + g_next[9] +
-                              g_next[10] + g_next[11] + g_next[12] + g_next[13] + g_next[14] +
-                              g_next[15] + g_next[16] + g_next[17] + g_next[18];
+            const float rho = d3q19_rho_native(g_next);
             psi = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
         }
         if (keep) fl_next = fl;
@@ -211,33 +211,32 @@ __global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args
         if (!(fl_cur & CELL_WALL)) {
             const int o = x + a.W * (y + a.H * z);
             float rho, ux, uy, uz;
-            d3q19_moments(g_cur, rho, ux, uy, uz);
+            d3q19_moments_native(g_cur, rho, ux, uy, uz);
             if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
+            const float inv_rt = 1.f / (rho * a.tau_inv);
             float ex = ux, ey = uy, ez = uz;
-            if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
-            if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
-            if (a.Fz != 0.f) ez = uz + a.Fz / (rho * a.tau_inv);
-            float IFx = 0.f, IFy = 0.f, IFz = 0.f;
+            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+            float ps[19];
 #pragma unroll
-            for (int k = 1; k < 19; k++) {
-                const int s = (r + d3_cz(k) + 3) % 3;
-                const float t = (k < 7 ? a.w1 : a.w7) *
-                                sp[s][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
-                if (d3_cx(k) > 0) IFx = IFx + t; else if (d3_cx(k) < 0) IFx = IFx - t;
-                if (d3_cy(k) > 0) IFy = IFy + t; else if (d3_cy(k) < 0) IFy = IFy - t;
-                if (d3_cz(k) > 0) IFz = IFz + t; else if (d3_cz(k) < 0) IFz = IFz - t;
-            }
-            const float gp = -a.G * sp[r % 3][ty + 1][tx + 1];
-            ex = ex + (gp * IFx) / (a.tau_inv * rho);
-            ey = ey + (gp * IFy) / (a.tau_inv * rho);
-            ez = ez + (gp * IFz) / (a.tau_inv * rho);
-            d3q19_bgk(g_cur, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+            for (int k = 0; k < 19; k++)
+                ps[k] = sp[(r + d3_cz(k) + 3) % 3][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
+            float IFx, IFy, IFz;
+            d3q19_sc_sum_native(ps, a.w1, a.w7, IFx, IFy, IFz);
+            const float c = (-a.G * ps[0]) * inv_rt;
+            ex = __fmaf_rn(c, IFx, ex);
+            ey = __fmaf_rn(c, IFy, ey);
+            ez = __fmaf_rn(c, IFz, ez);
+            d3q19_bgk_native(g_cur, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
             S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
             for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g_cur[k], a.wr[k]);
-        } else if (MOM) {
+        } else {
             const int o = x + a.W * (y + a.H * z);
-            a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f;
+            if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int k = 0; k < 19; k++) g_cur[k] = g_next[k];

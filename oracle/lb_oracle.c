@@ -66,15 +66,19 @@ float lbo_expf(float x)
 
 #define R float
 #define S f32
+#define FMA_R fmaf
 #include "lb_oracle_body.h"
 #undef R
 #undef S
+#undef FMA_R
 
 #define R double
 #define S f64
+#define FMA_R fma
 #include "lb_oracle_body.h"
 #undef R
 #undef S
+#undef FMA_R
 
 /* solid_bound = node and all 8 neighbours solid, for x in 1..W-2 only and
  * periodic in y (src/simulation_d2q9.cu:318-334) */

@@ -84,6 +84,71 @@ static inline void FN(d3q19_moments)(const R *g, R *rho, R *ux, R *uy, R *uz)
     *uz = (g[5] + g[9] + g[13] + g[15] + g[17] - g[6] - g[10] - g[14] - g[16] - g[18]) / r;
 }
 
+/* ---- native mode (no reference counterpart): the library's association and
+ * fused multiply-adds (FMA_R = fmaf / fma, one rounding like the GPU's)
+ * lattibol_0.3.31f_gb300/csrc/lb_common.cuh, d3q19_*_native */
+static inline void FN(d3q19_xsums_native)(const R *g, R *px, R *mx, R *zx)
+{
+    *px = (g[1] + g[7]) + (g[8] + g[9]) + g[10];
+    *mx = (g[2] + g[11]) + (g[12] + g[13]) + g[14];
+    *zx = ((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17])) + g[18];
+}
+static inline R FN(d3q19_rho_native)(const R *g)
+{
+    R px, mx, zx;
+    FN(d3q19_xsums_native)(g, &px, &mx, &zx);
+    return (px + mx) + zx;
+}
+static inline void FN(d3q19_moments_native)(const R *g, R *rho, R *ux, R *uy, R *uz)
+{
+    R px, mx, zx;
+    FN(d3q19_xsums_native)(g, &px, &mx, &zx);
+    const R r = (px + mx) + zx;
+    const R jy = ((g[3] + g[7]) + (g[11] + g[15]) + g[16]) -
+                 ((g[4] + g[8]) + (g[12] + g[17]) + g[18]);
+    const R jz = ((g[5] + g[9]) + (g[13] + g[15]) + g[17]) -
+                 ((g[6] + g[10]) + (g[14] + g[16]) + g[18]);
+    const R inv = (R)1 / r;
+    *rho = r;
+    *ux = (px - mx) * inv;
+    *uy = jy * inv;
+    *uz = jz * inv;
+}
+static inline void FN(bgk_pair_native)(R *g, int kp, int km, R a, R p, R base, R tau_inv)
+{
+    const R t = FMA_R((R)4.5f * p, p, base);
+    const R fp = a * FMA_R((R)3.f, p, t), fm = a * FMA_R((R)-3.f, p, t);
+    g[kp] = FMA_R(tau_inv, fp - g[kp], g[kp]);
+    g[km] = FMA_R(tau_inv, fm - g[km], g[km]);
+}
+static inline void FN(d3q19_bgk_native)(R *g, R ux, R uy, R uz, R rho, R w0, R w1, R w7,
+                                        R tau_inv)
+{
+    const R usq = FMA_R(uz, uz, FMA_R(uy, uy, ux * ux));
+    const R base = FMA_R((R)-1.5f, usq, (R)1.f);
+    const R a0 = w0 * rho, a1 = w1 * rho, a7 = w7 * rho;
+    g[0] = FMA_R(tau_inv, a0 * base - g[0], g[0]);
+    FN(bgk_pair_native)(g, 1, 2, a1, ux, base, tau_inv);
+    FN(bgk_pair_native)(g, 3, 4, a1, uy, base, tau_inv);
+    FN(bgk_pair_native)(g, 5, 6, a1, uz, base, tau_inv);
+    FN(bgk_pair_native)(g, 7, 12, a7, ux + uy, base, tau_inv);
+    FN(bgk_pair_native)(g, 8, 11, a7, ux - uy, base, tau_inv);
+    FN(bgk_pair_native)(g, 9, 14, a7, ux + uz, base, tau_inv);
+    FN(bgk_pair_native)(g, 10, 13, a7, ux - uz, base, tau_inv);
+    FN(bgk_pair_native)(g, 15, 18, a7, uy + uz, base, tau_inv);
+    FN(bgk_pair_native)(g, 16, 17, a7, uy - uz, base, tau_inv);
+}
+/* ps[k] = psi(x + c_k) */
+static inline void FN(d3q19_sc_sum_native)(const R *ps, R w1, R w7, R *IFx, R *IFy, R *IFz)
+{
+    *IFx = FMA_R(w1, ps[1] - ps[2],
+                 w7 * (((ps[7] + ps[8]) + (ps[9] + ps[10])) - ((ps[11] + ps[12]) + (ps[13] + ps[14]))));
+    *IFy = FMA_R(w1, ps[3] - ps[4],
+                 w7 * (((ps[7] + ps[11]) + (ps[15] + ps[16])) - ((ps[8] + ps[12]) + (ps[17] + ps[18]))));
+    *IFz = FMA_R(w1, ps[5] - ps[6],
+                 w7 * (((ps[9] + ps[13]) + (ps[15] + ps[17])) - ((ps[10] + ps[14]) + (ps[16] + ps[18]))));
+}
+
 /* Zou-He velocity inlet (west), src/collision.cu:412-430 */
 static inline void FN(d3q19_zou_he_west)(R *g, R ux_in)
 {
@@ -383,11 +448,12 @@ void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *u
 #pragma omp parallel for schedule(static)
         for (long o = 0; o < N; o++) {
             if (flags[o] & LBO_SOLID) { psi[o] = 0; continue; }
-            R r = 0;
-            /* post-stream density = sum over the slots after the local swap */
-            r = f[0 * N + o];
-            for (int k = 1; k < 19; k++) r = r + f[D3_OPP[k] * N + o];
-            psi[o] = FN(psi_of)(r, psi_form);
+            /* post-stream populations sit in the opposite slots before the
+             * local swap; the density in the native moments' association */
+            R g[19];
+            g[0] = f[o];
+            for (int k = 1; k < 19; k++) g[k] = f[D3_OPP[k] * N + o];
+            psi[o] = FN(psi_of)(FN(d3q19_rho_native)(g), psi_form);
         }
     }
 #pragma omp parallel for schedule(static)
@@ -403,29 +469,29 @@ void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *u
             R t = g[k]; g[k] = g[q]; g[q] = t;
         }
         R r, vx, vy, vz;
-        FN(d3q19_moments)(g, &r, &vx, &vy, &vz);
+        FN(d3q19_moments_native)(g, &r, &vx, &vy, &vz);
         R ex = vx, ey = vy, ez = vz;
-        if (Fx != 0) ex = vx + Fx / (r * tau_inv);
-        if (Fy != 0) ey = vy + Fy / (r * tau_inv);
-        if (Fz != 0) ez = vz + Fz / (r * tau_inv);
-        if (sc) {
-            const int x = (int)(o % W), y = (int)((o / W) % H), z = (int)(o / ((long)W * H));
-            R IFx = 0, IFy = 0, IFz = 0;
-            for (int k = 1; k < 19; k++) {
-                const long on = wrapi(x + D3_CX[k], W) + (long)wrapi(y + D3_CY[k], H) * W +
-                                (long)wrapi(z + D3_CZ[k], D) * W * H;
-                const R t = (k < 7 ? w1 : w7) * psi[on];
-                if (D3_CX[k] > 0) IFx = IFx + t; else if (D3_CX[k] < 0) IFx = IFx - t;
-                if (D3_CY[k] > 0) IFy = IFy + t; else if (D3_CY[k] < 0) IFy = IFy - t;
-                if (D3_CZ[k] > 0) IFz = IFz + t; else if (D3_CZ[k] < 0) IFz = IFz - t;
+        if (sc || Fx != 0 || Fy != 0 || Fz != 0) {
+            const R inv_rt = (R)1 / (r * tau_inv);
+            if (Fx != 0) ex = FMA_R(Fx, inv_rt, vx);
+            if (Fy != 0) ey = FMA_R(Fy, inv_rt, vy);
+            if (Fz != 0) ez = FMA_R(Fz, inv_rt, vz);
+            if (sc) {
+                const int x = (int)(o % W), y = (int)((o / W) % H), z = (int)(o / ((long)W * H));
+                R ps[19];
+                for (int k = 0; k < 19; k++)
+                    ps[k] = psi[wrapi(x + D3_CX[k], W) + (long)wrapi(y + D3_CY[k], H) * W +
+                                (long)wrapi(z + D3_CZ[k], D) * W * H];
+                R IFx, IFy, IFz;
+                FN(d3q19_sc_sum_native)(ps, w1, w7, &IFx, &IFy, &IFz);
+                const R c = (-G * ps[0]) * inv_rt;
+                ex = FMA_R(c, IFx, ex);
+                ey = FMA_R(c, IFy, ey);
+                ez = FMA_R(c, IFz, ez);
             }
-            const R gp = -G * psi[o];
-            ex = ex + (gp * IFx) / (tau_inv * r);
-            ey = ey + (gp * IFy) / (tau_inv * r);
-            ez = ez + (gp * IFz) / (tau_inv * r);
         }
         if (rho) { ux[o] = vx; uy[o] = vy; uz[o] = vz; rho[o] = r; }
-        FN(d3q19_bgk)(g, ex, ey, ez, r, w0, w1, w7, tau_inv);
+        FN(d3q19_bgk_native)(g, ex, ey, ez, r, w0, w1, w7, tau_inv);
         for (int k = 0; k < 19; k++) f[k * N + o] = g[k];
     }
 }
