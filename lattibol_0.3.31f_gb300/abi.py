@@ -178,6 +178,7 @@ PROTOTYPES = [
     ("lb_device_fields", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_void_p)] * 4),
     ("lb_extents", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3),
     ("lb_tcgen05_selftest", _c.c_int, [_c.c_void_p, _c.POINTER(_c.c_int)]),
+    ("lb_wait_selftest", _c.c_int, [_c.c_int, _c.POINTER(_c.c_int)]),
     ("lb_case_load_parameters", _c.c_int, [_c.c_char_p, _c.POINTER(lb_case_params)]),
     ("lb_case_load_solids_bmp", _c.c_int, [_c.c_char_p, _c.POINTER(_c.c_int),
                                            _c.POINTER(_c.c_int), _c.c_void_p, _c.c_size_t]),

@@ -273,8 +273,8 @@ __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
 
 // true once *flag >= target; false when this wait gave up (it then raises
 // *err) or another block already has
-__device__ bool wait_band(const int *flag, int target, int *err) {
-    for (int i = 0; i < PERSIST_SPIN_LIMIT; i++) {
+__device__ bool wait_band(const int *flag, int target, int *err, int limit = PERSIST_SPIN_LIMIT) {
+    for (int i = 0; i < limit; i++) {
         if (ld_acquire_gpu(flag) >= target) return true;
         if ((i & 63) == 63) {
             if (ld_acquire_gpu(err) != 0) return false;
@@ -377,6 +377,17 @@ __global__ void __launch_bounds__(1024) d2q9_persistent_kernel(const D2Args a, i
         __syncthreads();
         if (give_up) return;
     }
+}
+
+// self-check of the bounded wait: block 0 waits for a band counter that no
+// block raises; it must give up after `limit` polls and raise sync[0]
+__global__ void band_wait_selftest_kernel(int *sync, int limit) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) wait_band(sync + 1, 1, sync, limit);
+}
+
+cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s) {
+    band_wait_selftest_kernel<<<2, 32, 0, s>>>(sync, limit);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_d2q9_persistent(const D2Args &a, int mode, int nsteps, int *sync,

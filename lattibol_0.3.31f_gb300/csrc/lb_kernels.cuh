@@ -91,6 +91,8 @@ cudaError_t launch_d2q9_fused_pdl(const D2Args &a, int mode, bool mom, cudaStrea
 // when the bands cannot all be resident.
 cudaError_t launch_d2q9_persistent(const D2Args &a, int mode, int nsteps, int *sync,
                                    cudaStream_t s);
+// self-check of the persistent loop's bounded wait (sync: 2 zeroed ints)
+cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s);
 cudaError_t launch_d2q9_stream_swap(const Pop<9> &p, const uint8_t *sb, int W, int H,
                                     cudaStream_t s);
 cudaError_t launch_d2q9_collide(const D2Args &a, bool plot, cudaStream_t s);

@@ -107,7 +107,49 @@ __global__ void __launch_bounds__(128) tc05_selftest_kernel(float *out, int *sta
     if (t == 0) mbar_inval(&mbar);
 }
 
+// self-check of the bounded mbarrier wait: nothing is committed to the
+// barrier, so the wait must give up after `limit` attempts; the block then
+// releases its tensor memory and reports
+__global__ void __launch_bounds__(128) tc05_wait_selftest_kernel(int *status, int limit) {
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int t = threadIdx.x, warp = t >> 5;
+    if (warp == 0) tc_alloc(&tslot, 32);
+    if (t == 0) mbar_init(&mbar, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const bool ok = __syncthreads_and(mbar_wait(&mbar, 0, limit));
+    if (!ok && t == 0) atomicExch(status, 1);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tslot, 32);
+    if (t == 0) mbar_inval(&mbar);
+}
+
 }  // namespace lb
+
+extern "C" int lb_wait_selftest(int which, int *status_host) {
+    if (!status_host || (which != 0 && which != 1)) return LB_ERR_ARG;
+    int *dev = nullptr;
+    cudaError_t e = cudaMalloc(&dev, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(dev, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) {
+        if (which == 0) {
+            e = lb::launch_band_wait_selftest(dev, 1 << 14, 0);
+        } else {
+            lb::tc05_wait_selftest_kernel<<<1, 128>>>(dev, 1 << 10);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(status_host, dev, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(dev);
+    if (e != cudaSuccess) {
+        lb::abi_record_error("lb_wait_selftest", cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    return LB_OK;
+}
 
 extern "C" int lb_tcgen05_selftest(float *out_host, int *status_host) {
     if (!out_host || !status_host) return LB_ERR_ARG;

@@ -26,3 +26,18 @@ def test_tcgen05_selftest_rounds(pkg):
         H = ((r + 3 * k64 + rd) % 5 - 2).astype(np.float64)
         assert np.array_equal(out[rd, 0], (X @ W1.T).astype(np.float32)), rd
         assert np.array_equal(out[rd, 1], (H @ W2.T).astype(np.float32)), rd
+
+
+@pytest.mark.parametrize("which", [0, 1], ids=["persistent_band_wait", "tcgen05_mbarrier_wait"])
+def test_bounded_waits_give_up_and_report(pkg, which):
+    """A wait on a flag that nothing sets (a band counter / an mbarrier with
+    nothing committed) runs out, raises the error word and returns; the GPU
+    stays usable (the layout self-check runs right after)."""
+    L = pkg.lib()
+    status = ctypes.c_int(-1)
+    assert L.lb_wait_selftest(which, ctypes.byref(status)) == 0, L.lb_abi_last_error()
+    assert status.value == 1
+    out = np.zeros((3, 2, 128, 64), np.float32)
+    st = ctypes.c_int(-1)
+    assert L.lb_tcgen05_selftest(out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(st)) == 0
+    assert st.value == 0
