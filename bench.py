@@ -102,7 +102,9 @@ WORKLOADS = {
         "cavity", 9, (256, 256, 1), 0.6, 10000, 2 * 9 * 4 + 1, wall_u=(0.1, 0, 0),
         describe={"lid_velocity": 0.1, "boundaries": "half-way bounce-back box, moving top wall",
                   "init": "equilibrium rho=1 u=0",
-                  "l2": "state (4.7 MB) fits L2: launch-latency bound, graph-replayed programmatic dependent launches"}),
+                  "l2": "state (4.7 MB) fits L2: temporal blocks of 5 steps per launch "
+                        "(32x14 tiles with their halo in shared memory), graph-replayed "
+                        "programmatic dependent launches"}),
 }
 # D3Q19 Shan-Chen spinodal decomposition, 256^3 periodic, tau = 1, G = -5,
 # psi = 1 - exp(-rho); algorithmic bytes/LU: populations read + written once,

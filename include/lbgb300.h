@@ -182,6 +182,12 @@ typedef enum {
 #define LB_TUNE_REVERSE 0x001  /* sweep the lattice in the opposite order on every
                                   other step, so a step starts where the previous
                                   one ended and its last writes are still in L2 */
+#define LB_TUNE_TBLOCK 0x020   /* D2Q9 native mode without Shan-Chen: temporal
+                                  blocking, one launch advances several steps of a
+                                  tile and its halo in shared memory */
+#define LB_TUNE_TBLOCK_SHAPE(n) ((n) << 12) /* with LB_TUNE_TBLOCK: block shape 1..10
+                                               (steps per launch x tile), 0 = the
+                                               library's choice */
 
 typedef struct {
     int lattice;        /* LB_D2Q9 or LB_D3Q19 */

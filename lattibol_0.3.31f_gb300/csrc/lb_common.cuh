@@ -286,6 +286,59 @@ __device__ __forceinline__ void d2q9_moments(const float (&g)[9], float &rho, fl
     uy = (g[2] - g[4] + g[5] + g[6] - g[7] - g[8]) / rho;
 }
 
+// ------------------------------------------- native-mode D2Q9 arithmetic
+// The same quantities as above in the library's own association (partial
+// sums by c_x shared between rho and j_x, one division for 1/rho) and with
+// fused multiply-adds in the BGK, as d3q19_*_native.  Native mode only; the
+// oracle performs the same operations (oracle/lb_oracle_body.h,
+// d2q9_*_native).
+__device__ __forceinline__ void d2q9_moments_native(const float (&g)[9], float &rho, float &ux,
+                                                    float &uy) {
+    const float px = (g[1] + g[5]) + g[8];  // c_x = +1
+    const float mx = (g[3] + g[6]) + g[7];  // c_x = -1
+    const float zx = (g[0] + g[2]) + g[4];  // c_x = 0
+    const float r = (px + mx) + zx;
+    const float jy = ((g[2] + g[5]) + g[6]) - ((g[4] + g[7]) + g[8]);
+    const float inv = 1.f / r;
+    rho = r;
+    ux = (px - mx) * inv;
+    uy = jy * inv;
+}
+
+__device__ __forceinline__ void d2q9_bgk_native(float (&g)[9], float ux, float uy, float rho,
+                                                float w0, float w1, float w5, float tau_inv) {
+    const float usq = __fmaf_rn(uy, uy, ux * ux);
+    const float base = __fmaf_rn(-1.5f, usq, 1.f);
+    const float a0 = w0 * rho, a1 = w1 * rho, a5 = w5 * rho;
+    g[0] = __fmaf_rn(tau_inv, a0 * base - g[0], g[0]);
+    auto pair = [&](int kp, int km, float a, float p) {
+        const float t = __fmaf_rn(4.5f * p, p, base);
+        const float fp = a * __fmaf_rn(3.f, p, t), fm = a * __fmaf_rn(-3.f, p, t);
+        g[kp] = __fmaf_rn(tau_inv, fp - g[kp], g[kp]);
+        g[km] = __fmaf_rn(tau_inv, fm - g[km], g[km]);
+    };
+    pair(1, 3, a1, ux);
+    pair(2, 4, a1, uy);
+    pair(5, 7, a5, ux + uy);
+    pair(6, 8, a5, uy - ux);
+}
+
+// native collision after the pull: moments, velocity-shift force with one
+// division 1/(rho tau_inv) (the form of reference src/collision.cu:280-284),
+// BGK; rho, ux, uy are the moments before the shift
+__device__ __forceinline__ void d2q9_collide_native(float (&g)[9], float Fx, float Fy, float w0,
+                                                    float w1, float w5, float tau_inv,
+                                                    float &rho, float &ux, float &uy) {
+    d2q9_moments_native(g, rho, ux, uy);
+    float ex = ux, ey = uy;
+    if (Fx != 0.f || Fy != 0.f) {
+        const float inv_rt = 1.f / (rho * tau_inv);
+        if (Fx != 0.f) ex = __fmaf_rn(Fx, inv_rt, ux);
+        if (Fy != 0.f) ey = __fmaf_rn(Fy, inv_rt, uy);
+    }
+    d2q9_bgk_native(g, ex, ey, rho, w0, w1, w5, tau_inv);
+}
+
 // Zou-He west inlet / east outlet, reference src/collision.cu:210-262
 __device__ __forceinline__ void d2q9_zou_he_west(float (&g)[9], float ux_in) {
     const float a = g[0] + g[2] + g[4], b = g[3] + g[7] + g[6];

@@ -68,9 +68,15 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
 // channel.  D2Q9: programmatic dependent launches measured 24.9 vs 22.7 GLUPS
 // on the 256^2 cavity (the alternating sweep: 23.8 with them); the persistent
 // loop measured 9.7 (each step waits on a chain of L2 round trips) and stays
-// opt-in.
+// opt-in.  Temporal blocks of 5 steps on 32x14 tiles (native mode without
+// Shan-Chen) measured 48.5 vs 24.1 GLUPS at 256^2, 11.1 vs 5.8 at 128^2 and
+// 73.3 vs 60.9 at 512^2, but 94.7 vs 101.5 at 1024^2 (a step then streams
+// from L2 faster than the blocks recompute their halos), so they are the
+// default up to TBLOCK_DEFAULT_MAX_NODES.
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE;
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D2 = LB_TUNE_PDL;
+constexpr int TBLOCK_DEFAULT_SHAPE = 5;
+constexpr long TBLOCK_DEFAULT_MAX_NODES = 1L << 19;
 
 const double W3[3] = {1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0};
 const double W2[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
@@ -122,6 +128,21 @@ bool sc_on(const lb_ctx *c) {
 // asks for it
 bool persistent_on(const lb_ctx *c) {
     return c->Q == 9 && !sc_on(c) && (c->tune & LB_TUNE_PERSISTENT);
+}
+
+// the temporal-blocking shape in effect (0 = per-step launches): D2Q9 native
+// mode without Shan-Chen, and the tuning asks for it
+int tblock_variant(const lb_ctx *c) {
+    if (c->Q != 9 || sc_on(c) || c->cfg.mode != LB_MODE_NATIVE || !(c->tune & LB_TUNE_TBLOCK))
+        return 0;
+    const int v = (c->tune >> 12) & 0x1f;
+    return tblock_steps(v) > 0 ? v : TBLOCK_DEFAULT_SHAPE;
+}
+
+// launches of temporal blocks per captured graph: even, so that a graph
+// returns to the set it started from
+int tblock_graph_launches(const lb_ctx *c, int steps_per_launch) {
+    return std::max(2, (c->cfg.graph_steps / steps_per_launch) & ~1);
 }
 
 // the step kernels write the cursor probe themselves (every step path does;
@@ -236,9 +257,18 @@ int graph_for(lb_ctx *c, int from, cudaGraphExec_t *out) {
            cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int set = from;
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < c->cfg.graph_steps && e == cudaSuccess; i++) {
-        e = step_once(c, set, false);
-        set = 1 - set;
+    const int tv = tblock_variant(c);
+    if (tv) {
+        const int L = tblock_graph_launches(c, tblock_steps(tv));
+        for (int i = 0; i < L && e == cudaSuccess; i++) {
+            e = launch_d2q9_tblock(d2_args(c, set), tv, false, c->stream);
+            set = 1 - set;
+        }
+    } else {
+        for (int i = 0; i < c->cfg.graph_steps && e == cudaSuccess; i++) {
+            e = step_once(c, set, false);
+            set = 1 - set;
+        }
     }
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
     c->launches = before;  // capture launches nothing
@@ -347,9 +377,12 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
     if (!(c->cfg.rho_ref > 0.f)) c->cfg.rho_ref = 1.f;
     c->tune = (cfg->tuning & LB_TUNE_EXPLICIT)
-                  ? (cfg->tuning & 0xff)
+                  ? (cfg->tuning & 0x1f0ff)
                   : (cfg->lattice == LB_D2Q9 ? LB_TUNE_LIBRARY_DEFAULT_D2
                                              : LB_TUNE_LIBRARY_DEFAULT_D3);
+    if (!(cfg->tuning & LB_TUNE_EXPLICIT) && cfg->lattice == LB_D2Q9 &&
+        N <= TBLOCK_DEFAULT_MAX_NODES)
+        c->tune |= LB_TUNE_TBLOCK | LB_TUNE_TBLOCK_SHAPE(TBLOCK_DEFAULT_SHAPE);
     c->Q = cfg->lattice;
     c->N = N;
     c->stride = (N + 127) / 128 * 128;  // every population array starts on a 256-byte boundary
@@ -526,6 +559,31 @@ int lb_step(lb_ctx *c, int nsteps) {
         if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported)
             return cuda_fail(c, "lb_step (persistent)", e);
         (void)cudaGetLastError();
+    }
+    if (const int tv = tblock_variant(c)) {
+        // temporal blocks of T steps (graphs of L blocks); the last block, or
+        // the last per-step launch of a remainder, writes the moments
+        const int T = tblock_steps(tv), L = tblock_graph_launches(c, T);
+        int rest = nsteps;
+        while (rest > L * T) {
+            cudaGraphExec_t g;
+            int rc = graph_for(c, c->cur, &g);
+            if (rc != LB_OK) return rc;
+            LB_TRY(c, "cudaGraphLaunch", cudaGraphLaunch(g, c->stream));
+            c->launches += L;
+            rest -= L * T;
+        }
+        for (; rest >= T; rest -= T) {
+            LB_TRY(c, "lb_step", launch_d2q9_tblock(d2_args(c, c->cur), tv, rest == T, c->stream));
+            c->launches += 1;
+            c->cur = 1 - c->cur;
+        }
+        for (; rest > 0; rest--) {
+            LB_TRY(c, "lb_step", step_once(c, c->cur, rest == 1));
+            c->cur = 1 - c->cur;
+        }
+        c->steps += nsteps;
+        return LB_OK;
     }
     int rest = nsteps - 1;  // the last step also writes the moment fields
     while (rest >= c->cfg.graph_steps) {

@@ -88,6 +88,16 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
 #pragma unroll
         for (int k = 0; k < 9; k++) g[k] = ld_stream(a.src.f[k] + o + n.off(-d2_cx(k), -d2_cr(k)));
     }
+    if (MODE == MODE_NATIVE && !SC) {
+        float rho, ux, uy;
+        d2q9_collide_native(g, a.Fx, a.Fy, a.w0, a.w1, a.w5, a.tau_inv, rho, ux, uy);
+        if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
+        if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
+        if (PLOT) a.plot[o] = make_float4(ux, uy, 0.f, rho);
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.dst.f[k][o] = g[k];
+        return;
+    }
     if (MODE == MODE_REF) {
         if (x == 0 && a.dev == 0)
             d2q9_zou_he_west(g, a.ux_in);
@@ -338,13 +348,17 @@ __device__ __forceinline__ void d2q9_node_l2(const D2Args &a, int par, int x, in
             d2q9_zou_he_east(g, a.rho_out);
     }
     float rho, ux, uy;
-    d2q9_moments(g, rho, ux, uy);
-    float ex = ux, ey = uy;
-    if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
-    if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
+    if (MODE == MODE_NATIVE) {
+        d2q9_collide_native(g, a.Fx, a.Fy, a.w0, a.w1, a.w5, a.tau_inv, rho, ux, uy);
+    } else {
+        d2q9_moments(g, rho, ux, uy);
+        float ex = ux, ey = uy;
+        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
+        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
+        d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, a.tau_inv);
+    }
     if (mom) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
     if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
-    d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, a.tau_inv);
 #pragma unroll
     for (int k = 0; k < 9; k++) dst[k][o] = g[k];
 }

@@ -138,6 +138,31 @@ static inline void FN(d3q19_bgk_native)(R *g, R ux, R uy, R uz, R rho, R w0, R w
     FN(bgk_pair_native)(g, 15, 18, a7, uy + uz, base, tau_inv);
     FN(bgk_pair_native)(g, 16, 17, a7, uy - uz, base, tau_inv);
 }
+/* native D2Q9 (lattibol_0.3.31f_gb300/csrc/lb_common.cuh, d2q9_*_native):
+ * partial sums by c_x, one division for 1/rho, the BGK pairs above */
+static inline void FN(d2q9_moments_native)(const R *g, R *rho, R *ux, R *uy)
+{
+    const R px = (g[1] + g[5]) + g[8];
+    const R mx = (g[3] + g[6]) + g[7];
+    const R zx = (g[0] + g[2]) + g[4];
+    const R r = (px + mx) + zx;
+    const R jy = ((g[2] + g[5]) + g[6]) - ((g[4] + g[7]) + g[8]);
+    const R inv = (R)1 / r;
+    *rho = r;
+    *ux = (px - mx) * inv;
+    *uy = jy * inv;
+}
+static inline void FN(d2q9_bgk_native)(R *g, R ux, R uy, R rho, R w0, R w1, R w5, R tau_inv)
+{
+    const R usq = FMA_R(uy, uy, ux * ux);
+    const R base = FMA_R((R)-1.5f, usq, (R)1.f);
+    const R a0 = w0 * rho, a1 = w1 * rho, a5 = w5 * rho;
+    g[0] = FMA_R(tau_inv, a0 * base - g[0], g[0]);
+    FN(bgk_pair_native)(g, 1, 3, a1, ux, base, tau_inv);
+    FN(bgk_pair_native)(g, 2, 4, a1, uy, base, tau_inv);
+    FN(bgk_pair_native)(g, 5, 7, a5, ux + uy, base, tau_inv);
+    FN(bgk_pair_native)(g, 6, 8, a5, uy - ux, base, tau_inv);
+}
 /* ps[k] = psi(x + c_k) */
 static inline void FN(d3q19_sc_sum_native)(const R *ps, R w1, R w7, R *IFx, R *IFy, R *IFz)
 {
@@ -521,9 +546,11 @@ void FN(lbo_d2q9_stream_native)(R *f, const uint8_t *flags, const R *corr, int W
         }
 }
 
-/* Native D2Q9 collision: the reference's two-pass structure (moments, psi,
- * u_eq; then the Shan-Chen pass) without Zou-He, with psi defined (0) at wall
- * cells, the psi form selectable, and the interaction applied for any G != 0. */
+/* Native D2Q9 collision.  Without Shan-Chen: the native arithmetic
+ * (d2q9_moments_native, d2q9_bgk_native).  With it: the reference's two-pass
+ * structure (moments, psi, u_eq; then the Shan-Chen pass) without Zou-He,
+ * with psi defined (0) at wall cells, the psi form selectable, and the
+ * interaction applied for any G != 0. */
 void FN(lbo_d2q9_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *rho, R *psi,
                                  int W, int H, R w0, R w1, R w5, R tau_inv, R Fx, R Fy, R G,
                                  R Gads, int psi_form)
@@ -553,6 +580,21 @@ void FN(lbo_d2q9_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *rh
             R t = g[k]; g[k] = g[q]; g[q] = t;
         }
         R r, vx, vy;
+        if (!sc) {
+            /* without Shan-Chen: the native arithmetic, one division for
+             * 1/(rho tau_inv) in the force shift */
+            FN(d2q9_moments_native)(g, &r, &vx, &vy);
+            R ex = vx, ey = vy;
+            if (Fx != 0 || Fy != 0) {
+                const R inv_rt = (R)1 / (r * tau_inv);
+                if (Fx != 0) ex = FMA_R(Fx, inv_rt, vx);
+                if (Fy != 0) ey = FMA_R(Fy, inv_rt, vy);
+            }
+            if (rho) { ux[o] = vx; uy[o] = vy; rho[o] = r; }
+            FN(d2q9_bgk_native)(g, ex, ey, r, w0, w1, w5, tau_inv);
+            for (int k = 0; k < 9; k++) f[k * N + o] = g[k];
+            continue;
+        }
         FN(d2q9_moments)(g, &r, &vx, &vy);
         R ex = vx, ey = vy;
         if (Fx != 0) ex = vx + Fx / (r * tau_inv);
