@@ -309,8 +309,9 @@ int lb_mlp_grad(lb_mlp *m, const float *x_dev, const float *z_dev, long n, float
 int lb_mlp_train(lb_mlp *m, const float *x_dev, const float *z_dev, long n, int steps,
                  int batch, float lr, uint64_t seed, float *loss_log);
 /* install the closure on a D3Q19 native FP32 context (m == NULL removes it);
- * the network must outlive its use; y_out_dev (optional, N floats) receives
- * the raw network output of every fluid cell at each step */
+ * the network must outlive its use; its biases and output layer are read at
+ * this call (call it again after further training); y_out_dev (optional, N
+ * floats) receives the raw network output of every fluid cell at each step */
 int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, float z_max,
                       float *y_out_dev);
 /* training data from a fine lattice's last-step moment fields: Favre box

@@ -160,7 +160,6 @@ struct TcSmem {
     uint8_t a[128 * MLP_H * 2];         // A: features (K 32) then the hidden layer (K 64)
     uint8_t w1[MLP_H * MLP_IN_PAD * 2]; // W1 [64][32], K-major core matrices
     uint8_t w2[MLP_H * MLP_H * 2];      // W2 [64][64]
-    float b1[MLP_H], b2[MLP_H], w3[MLP_H], b3;
     uint64_t mbar;
     uint32_t tslot;
 };
@@ -176,15 +175,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
     for (int i = t; i < MLP_H * MLP_H; i += D3_BLOCK)
         *reinterpret_cast<__nv_bfloat16 *>(sm.w2 + kmajor_offset(i / MLP_H, i % MLP_H, MLP_H)) =
             ca.mlp.w2[i];
-    for (int i = t; i < MLP_H; i += D3_BLOCK) {
-        sm.b1[i] = ca.mlp.b1[i];
-        sm.b2[i] = ca.mlp.b2[i];
-        sm.w3[i] = ca.mlp.w3[i];
-    }
-    if (t == 0) {
-        sm.b3 = ca.mlp.b3[0];
-        mbar_init(&sm.mbar, 1);
-    }
+    if (t == 0) mbar_init(&sm.mbar, 1);
     if (warp == 0) tc_alloc(&sm.tslot, TC_COLS);
     fence_proxy_async();
     tc_fence_before();
@@ -197,13 +188,14 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
     uint32_t phase = 0;
     bool ok = true;
 
+    // row-blocks r = bx + nbx (y + H z); 32-bit: a lattice has fewer than
+    // 2^31 of them (the node count itself is below 2^31)
     const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
-    const long nrows = (long)nbx * a.H * a.D;
-    for (long r = blockIdx.x; r < nrows && ok; r += gridDim.x) {
-        const long rr = a.reverse ? nrows - 1 - r : r;
-        const int bx = (int)(rr % nbx);
-        const long yz = rr / nbx;
-        const int y = (int)(yz % a.H), z = (int)(yz / a.H);
+    const int nrows = nbx * a.H * a.D;
+    for (int r = blockIdx.x; r < nrows && ok; r += gridDim.x) {
+        const int rr = a.reverse ? nrows - 1 - r : r;
+        const int bx = rr % nbx, yz = rr / nbx;
+        const int y = yz % a.H, z = yz / a.H;
         const int x = bx * D3_BLOCK + t;
         const bool inside = x < a.W;
         const int o = inside ? x + a.W * (y + a.H * z) : 0;
@@ -244,7 +236,10 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
                             tc_desc(w1_addr + 256 * s, 128, MLP_IN_PAD / 8 * 128), id, s > 0);
             tc_commit(&sm.mbar);
         }
-        ok = __syncthreads_and(mbar_wait(&sm.mbar, phase, TC_WAIT));
+        // thread 0 polls the mbarrier; the others wait at the block barrier
+        // (no issue slots), which with tcgen05.fence::after_thread_sync
+        // orders their tensor-memory loads after the MMA's completion
+        ok = __syncthreads_and(t == 0 ? mbar_wait(&sm.mbar, phase, TC_WAIT) : true);
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
@@ -259,8 +254,8 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int q = 8 * h + 2 * j;
-                    p[j] = __floats2bfloat162_rn(fmaxf(v[q] + sm.b1[c + q], 0.f),
-                                                 fmaxf(v[q + 1] + sm.b1[c + q + 1], 0.f));
+                    p[j] = __floats2bfloat162_rn(fmaxf(v[q] + ca.head_b1[c + q], 0.f),
+                                                 fmaxf(v[q + 1] + ca.head_b1[c + q + 1], 0.f));
                 }
                 *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, c + 8 * h, MLP_H)) =
                     *reinterpret_cast<const uint4 *>(p);
@@ -278,7 +273,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
                             tc_desc(w2_addr + 256 * s, 128, MLP_H / 8 * 128), id, s > 0);
             tc_commit(&sm.mbar);
         }
-        ok = __syncthreads_and(mbar_wait(&sm.mbar, phase, TC_WAIT));
+        ok = __syncthreads_and(t == 0 ? mbar_wait(&sm.mbar, phase, TC_WAIT) : true);
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
@@ -289,9 +284,10 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
             float v[32];
             tc_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
-            for (int j = 0; j < 32; j++) yv = yv + sm.w3[c + j] * fmaxf(v[j] + sm.b2[c + j], 0.f);
+            for (int j = 0; j < 32; j++)
+                yv = yv + ca.head_w3[c + j] * fmaxf(v[j] + ca.head_b2[c + j], 0.f);
         }
-        yv = yv + sm.b3;
+        yv = yv + ca.head_b3;
         tc_fence_before();  // the next run's MMA overwrites these columns after a barrier
         if (!inside) continue;
         if (!fluid) {
@@ -787,6 +783,13 @@ int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, floa
     if (!(nu0 > 0.f) || !(s_ref > 0.f) || !(z_max >= 0.f)) return LB_ERR_ARG;
     ClosureArgs ca{};
     ca.mlp = mlp_dev(m);
+    cudaError_t e = cudaSuccess;
+    const std::pair<float *, int> head[4] = {{ca.head_b1, MLP_OFF_B1}, {ca.head_b2, MLP_OFF_B2},
+                                             {ca.head_w3, MLP_OFF_W3}, {&ca.head_b3, MLP_OFF_B3}};
+    for (int i = 0; i < 4 && e == cudaSuccess; i++)
+        e = cudaMemcpy(head[i].first, m->p + head[i].second,
+                       sizeof(float) * (i == 3 ? 1 : MLP_H), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return LB_ERR_CUDA;
     ca.nu0 = nu0;
     ca.tau0 = 0.5f + 3.f * nu0;
     ca.s_ref = s_ref;

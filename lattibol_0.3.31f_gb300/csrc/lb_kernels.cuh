@@ -133,6 +133,10 @@ void abi_record_error(const char *where, const char *what);
 // learned closure (lb_closure.cu): the network and its scalings
 struct ClosureArgs {
     MlpDev mlp;
+    // b1, b2, w3, b3 by value: the tensor-core kernel reads them as constant
+    // operands of its epilogue instructions (a snapshot taken when the closure
+    // is enabled)
+    float head_b1[MLP_H], head_b2[MLP_H], head_w3[MLP_H], head_b3;
     float nu0, tau0, s_ref, z_max;
     float *y_out;     // optional: network output per cell (tests)
     int *err;         // device error word (tcgen05 kernel: an MMA that never completed)
