@@ -273,10 +273,15 @@ int lb_ensemble_init_equilibrium(lb_ensemble *e, const float *rho);
 int lb_ensemble_step(lb_ensemble *e, int nsteps);  /* last step writes the moments */
 int lb_ensemble_time_steps(lb_ensemble *e, int nsteps, float *ms);
 int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy);
-/* launch shape: threads along x (multiple of 32), rows per work item, blocks
- * per SM; the autotuner times every candidate for trial_steps steps on the
- * ensemble itself (advancing its state: tune before initialising) and keeps
- * the fastest, returned in out[3] */
+/* launch shape.  threads_x = 0: one launch per step over tiles that form psi
+ * of the tile and its ring in shared memory; rows then picks the tile shape
+ * (1: 32 x 8 at 48 registers, the default with 5 blocks per SM; 2: 32 x 8 at
+ * 40; 3: 32 x 16 at 60; 4: 32 x 16 at 40; 5: 32 x 32 at 60).  Otherwise the
+ * two-pass step (psi pass, fused pass)
+ * over groups of `rows` rows with threads_x threads along x (a multiple of
+ * 32).  Both give the same bits.  The autotuner times every candidate for
+ * trial_steps steps on the ensemble itself (advancing its state: tune before
+ * initialising) and keeps the fastest, returned in out[3] */
 int lb_ensemble_set_launch(lb_ensemble *e, int threads_x, int rows, int blocks_per_sm);
 int lb_ensemble_get_launch(const lb_ensemble *e, int out[3]);
 int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]);

@@ -40,6 +40,7 @@ struct EnsDomain {
 struct EnsItem {
     int off, W, H, y;
     float G, tau_inv;
+    int x;  // single-pass tiles: first column of the tile (0 for row groups)
 };
 
 struct EnsArgs {
@@ -126,8 +127,218 @@ __global__ void ens_fused_kernel(const EnsArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Single-pass step over tiles of 32 x BY nodes (the default launch).  A
+// block pulls its tile nodes (one per thread) and the ring of nodes around
+// them (84 for 32 x 8 tiles), forms psi of all of them in shared memory, and then relaxes
+// its tile nodes with the Shan-Chen shift from the shared psi tile.  psi never
+// goes through DRAM and a step is one launch: 72 B per node update moved
+// (populations read and written once; the ring's pulls are L2 hits of the
+// neighbouring tiles) instead of the two passes' 116.  The arithmetic is the
+// two-pass path's (same pulls, moments, psi, stencil order, BGK).
+// ---------------------------------------------------------------------------
+constexpr int ET_BX = 32, ET_PX = ET_BX + 2;  // tile width; psi tile width with its ring
+
+// v modulo n for v in [-n, 2n) (fast) or any v (small domains)
+__device__ __forceinline__ int ens_wrap(int v, int n, bool small) {
+    if (small) {
+        v %= n;
+        return v < 0 ? v + n : v;
+    }
+    return v < 0 ? v + n : (v >= n ? v - n : v);
+}
+
+// tiles of ET_BX x BY nodes, one thread per tile node; MINB resident blocks
+// per SM bound the registers
+template <int BY, int MINB, bool MOM>
+__global__ void __launch_bounds__(ET_BX * BY, MINB) ens_tile_kernel(const EnsArgs a) {
+    constexpr int PY = BY + 2, RING = 2 * ET_PX + 2 * BY;
+    // two psi tiles used by alternate items: a block passes one barrier per
+    // item (a warp writing tile b for item i + 2 has passed the barrier of
+    // item i + 1, which every warp reaches only after its reads of item i)
+    __shared__ float sp2[2][PY][ET_PX];
+    const int tx = threadIdx.x % ET_BX, ty = threadIdx.x / ET_BX;
+    // this thread's ring node, as a position in the psi tile
+    int rx = 0, ry = 0;
+    {
+        const int r = threadIdx.x;
+        if (r < ET_PX) { rx = r; ry = 0; }
+        else if (r < 2 * ET_PX) { rx = r - ET_PX; ry = PY - 1; }
+        else if (r < 2 * ET_PX + BY) { rx = 0; ry = 1 + r - 2 * ET_PX; }
+        else { rx = ET_PX - 1; ry = 1 + r - 2 * ET_PX - BY; }
+    }
+    int it = blockIdx.x;
+    if (it >= a.nitems) return;
+    EnsItem next = a.items[it];
+    for (int b = 0; it < a.nitems; it += gridDim.x, b ^= 1) {
+        float (*sp)[ET_PX] = sp2[b];
+        const EnsItem dm = next;
+        const int nit = it + gridDim.x;
+        if (nit < a.nitems) next = a.items[nit];
+        const bool small = dm.W < ET_PX || dm.H < PY;
+        // the tile node (a wrapped copy where the tile overhangs the domain);
+        // the ring node's loads are issued before either density is formed
+        const int xt = ens_wrap(dm.x + tx, dm.W, small), yt = ens_wrap(dm.y + ty, dm.H, small);
+        const bool ring = threadIdx.x < RING;
+        float g[9], g2[9];
+        ens_pull(a, dm, xt, yt, g);
+        if (ring)
+            ens_pull(a, dm, ens_wrap(dm.x - 1 + rx, dm.W, small),
+                     ens_wrap(dm.y - 1 + ry, dm.H, small), g2);
+        float rho, ux, uy;
+        d2q9_moments(g, rho, ux, uy);
+        sp[ty + 1][tx + 1] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+        if (ring) {
+            float r2, u2, v2;
+            d2q9_moments(g2, r2, u2, v2);
+            sp[ry][rx] = a.psi_form == 0 ? psi_ref(r2) : psi_exp1(r2);
+        }
+        __syncthreads();
+        if (dm.x + tx < dm.W && dm.y + ty < dm.H) {
+            // psi(x), psi(x+1,y), psi(x,row+1), psi(x-1,y), psi(x,row-1), then
+            // the diagonals: the fused pass's order
+            const float ps[9] = {sp[ty + 1][tx + 1], sp[ty + 1][tx + 2], sp[ty + 2][tx + 1],
+                                 sp[ty + 1][tx],     sp[ty][tx + 1],     sp[ty + 2][tx + 2],
+                                 sp[ty + 2][tx],     sp[ty][tx],         sp[ty][tx + 2]};
+            float ex = ux, ey = uy;
+            d2q9_sc_shift(ps, a.w1, a.w5, dm.G, dm.tau_inv, rho, ex, ey);
+            d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, dm.tau_inv);
+            const int o = dm.off + xt + dm.W * yt;
+            if (MOM) { a.rho[o] = rho; a.ux[o] = ux; a.uy[o] = uy; }
+#pragma unroll
+            for (int k = 0; k < 9; k++) a.dst[k][o] = g[k];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Single pass by warps marching down 32-column strips: no block barrier.  A
+// work item is a strip of 32 columns and R rows of one domain, and lane l owns
+// column x0 + l (a wrapped copy where the strip overhangs the domain).  For
+// each row r the warp pulls row r + 1 and forms its psi (lanes 0 and 31 also
+// psi of the columns x0 - 1 and x0 + 32), then relaxes row r with the psi
+// stencil of rows r - 1, r, r + 1 from its registers and its neighbour lanes.
+// Per node update that is 1 + 2/R + 2/32 pulls instead of the tiles' 1.33.
+// Same arithmetic and stencil order as the two-pass step.
+// ---------------------------------------------------------------------------
+constexpr int ENS_MARCH_THREADS = 256;
+
+__device__ __forceinline__ float ens_psi(const EnsArgs &a, float rho) {
+    return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+}
+
+template <int R, int MINB, bool MOM>
+__global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(const EnsArgs a) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int warps_per_block = ENS_MARCH_THREADS / 32;
+    const int nwarps = gridDim.x * warps_per_block;
+    const bool edge = lane == 0 || lane == 31;
+    for (int it = blockIdx.x * warps_per_block + (threadIdx.x >> 5); it < a.nitems;
+         it += nwarps) {
+        const EnsItem dm = a.items[it];
+        const bool small = dm.W < ET_PX;
+        const int x = ens_wrap(dm.x + lane, dm.W, small);
+        const int xh = ens_wrap(lane == 0 ? dm.x - 1 : dm.x + ET_BX, dm.W, small);
+        const bool own = dm.x + lane < dm.W;
+        const int y_end = min(dm.y + R, dm.H);
+        float gc[9], rc, uxc, uyc;  // row r: pulled populations and moments at x
+        float pm, pc, hm = 0.f, hc = 0.f;  // psi of rows r - 1, r (h: the halo column)
+        {
+            float g[9], r0, u0, v0;
+            const int ym = ens_wrap(dm.y - 1, dm.H, false);
+            ens_pull(a, dm, x, ym, g);
+            d2q9_moments(g, r0, u0, v0);
+            pm = ens_psi(a, r0);
+            ens_pull(a, dm, x, dm.y, gc);
+            d2q9_moments(gc, rc, uxc, uyc);
+            pc = ens_psi(a, rc);
+            if (edge) {
+                ens_pull(a, dm, xh, ym, g);
+                d2q9_moments(g, r0, u0, v0);
+                hm = ens_psi(a, r0);
+                ens_pull(a, dm, xh, dm.y, g);
+                d2q9_moments(g, r0, u0, v0);
+                hc = ens_psi(a, r0);
+            }
+        }
+        for (int r = dm.y; r < y_end; r++) {
+            const int yp = ens_wrap(r + 1, dm.H, false);
+            float gn[9], rn, uxn, uyn, hn = 0.f;
+            ens_pull(a, dm, x, yp, gn);
+            if (edge) {
+                float g[9], r0, u0, v0;
+                ens_pull(a, dm, xh, yp, g);
+                d2q9_moments(g, r0, u0, v0);
+                hn = ens_psi(a, r0);
+            }
+            d2q9_moments(gn, rn, uxn, uyn);
+            const float pn = ens_psi(a, rn);
+            // x - 1 and x + 1 from the neighbour lanes, the halo at the strip ends
+            float lm = __shfl_up_sync(FULL, pm, 1), lc = __shfl_up_sync(FULL, pc, 1);
+            float ln = __shfl_up_sync(FULL, pn, 1);
+            float qm = __shfl_down_sync(FULL, pm, 1), qc = __shfl_down_sync(FULL, pc, 1);
+            float qn = __shfl_down_sync(FULL, pn, 1);
+            if (lane == 0) { lm = hm; lc = hc; ln = hn; }
+            if (lane == 31) { qm = hm; qc = hc; qn = hn; }
+            if (own) {
+                // the fused pass's order: psi(x), psi(x+1,y), psi(x,row+1),
+                // psi(x-1,y), psi(x,row-1), then the diagonals
+                const float ps[9] = {pc, qc, pn, lc, pm, qn, ln, lm, qm};
+                float ex = uxc, ey = uyc;
+                d2q9_sc_shift(ps, a.w1, a.w5, dm.G, dm.tau_inv, rc, ex, ey);
+                d2q9_bgk(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
+                const int o = dm.off + x + dm.W * r;
+                if (MOM) { a.rho[o] = rc; a.ux[o] = uxc; a.uy[o] = uyc; }
+#pragma unroll
+                for (int k = 0; k < 9; k++) a.dst[k][o] = gc[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 9; k++) gc[k] = gn[k];
+            rc = rn; uxc = uxn; uyc = uyn;
+            pm = pc; pc = pn; hm = hc; hc = hn;
+        }
+    }
+}
+
+// march shapes: rows per item and the register bound (resident blocks per SM)
+#define LB_ENS_MARCH(X) \
+    X(6, 32, 3)         \
+    X(7, 32, 4)         \
+    X(8, 64, 3)         \
+    X(9, 16, 3)
+
+int ens_march_rows(int shape) {
+    switch (shape) {
+#define LB_ENS_MROWS(S, R, MINB) \
+    case S: return R;
+        LB_ENS_MARCH(LB_ENS_MROWS)
+#undef LB_ENS_MROWS
+        default: return 0;
+    }
+}
+
+// tile shapes: rows per tile and the register bound (resident blocks per SM)
+#define LB_ENS_TILES(X) \
+    X(1, 8, 5)          \
+    X(2, 8, 6)          \
+    X(3, 16, 2)         \
+    X(4, 16, 3)         \
+    X(5, 32, 1)
+
+int ens_tile_rows(int shape) {
+    switch (shape) {
+#define LB_ENS_ROWS(S, BY, MINB) \
+    case S: return BY;
+        LB_ENS_TILES(LB_ENS_ROWS)
+#undef LB_ENS_ROWS
+        default: return 0;
+    }
+}
+
 struct LaunchShape {
-    int bx, ry, bps;  // threads along x, rows per work item (= blockDim.y), blocks per SM
+    int bx, ry, bps;  // threads along x, rows per work item (= blockDim.y), blocks per SM;
+                      // bx = 0: the single-pass tile kernel of tile shape ry
 };
 
 }  // namespace
@@ -141,7 +352,7 @@ struct lb_ensemble {
     EnsItem *items_d = nullptr;
     int nitems = 0, items_cap = 0;
     int cur = 0, psi_form = LB_PSI_EXP1, sms = 1, graph_steps = 32;
-    LaunchShape shape{128, 1, 4};
+    LaunchShape shape{0, 1, 5};  // single-pass 32 x 8 tiles, 5 blocks per SM (48 registers)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -181,10 +392,33 @@ EnsArgs args_for(lb_ensemble *e, int from) {
     return a;
 }
 
+int launches_per_step(const lb_ensemble *e) { return e->shape.bx == 0 ? 1 : 2; }
+
 cudaError_t ens_step(lb_ensemble *e, int from, bool mom) {
     const EnsArgs a = args_for(e, from);
-    const dim3 block(e->shape.bx, e->shape.ry);
     const unsigned grid = (unsigned)std::max(1, std::min(e->nitems, e->sms * e->shape.bps));
+    if (e->shape.bx == 0) {
+        switch (e->shape.ry) {
+#define LB_ENS_LAUNCH(S, BY, MINB)                                                            \
+    case S:                                                                                   \
+        if (mom) ens_tile_kernel<BY, MINB, true><<<grid, ET_BX * BY, 0, e->stream>>>(a);    \
+        else ens_tile_kernel<BY, MINB, false><<<grid, ET_BX * BY, 0, e->stream>>>(a);       \
+        break;
+            LB_ENS_TILES(LB_ENS_LAUNCH)
+#undef LB_ENS_LAUNCH
+#define LB_ENS_MLAUNCH(S, R, MINB)                                                             \
+    case S:                                                                                    \
+        if (mom) ens_march_kernel<R, MINB, true><<<grid, ENS_MARCH_THREADS, 0, e->stream>>>(a); \
+        else ens_march_kernel<R, MINB, false><<<grid, ENS_MARCH_THREADS, 0, e->stream>>>(a);    \
+        break;
+            LB_ENS_MARCH(LB_ENS_MLAUNCH)
+#undef LB_ENS_MLAUNCH
+            default: return cudaErrorInvalidValue;
+        }
+        e->launches += 1;
+        return cudaGetLastError();
+    }
+    const dim3 block(e->shape.bx, e->shape.ry);
     ens_density_kernel<<<grid, block, 0, e->stream>>>(a);
     cudaError_t c = cudaGetLastError();
     if (c != cudaSuccess) return c;
@@ -205,11 +439,18 @@ void drop_graphs(lb_ensemble *e) {
 // work list of row groups for the current shape
 int build_items(lb_ensemble *e) {
     std::vector<EnsItem> items;
-    for (int d = 0; d < e->nd; d++)
-        for (int y = 0; y < e->dom[d].H; y += e->shape.ry) {
-            const EnsDomain &m = e->dom[d];
-            items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv});
+    for (int d = 0; d < e->nd; d++) {
+        const EnsDomain &m = e->dom[d];
+        if (e->shape.bx == 0) {  // tiles or strips, row by row
+            const int rows = ens_tile_rows(e->shape.ry) + ens_march_rows(e->shape.ry);
+            for (int y = 0; y < m.H; y += rows)
+                for (int x = 0; x < m.W; x += ET_BX)
+                    items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, x});
+        } else {  // groups of ry rows
+            for (int y = 0; y < m.H; y += e->shape.ry)
+                items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, 0});
         }
+    }
     if ((int)items.size() > e->items_cap) {
         if (e->items_d) cudaFree(e->items_d);
         e->items_d = nullptr;
@@ -355,7 +596,7 @@ int lb_ensemble_step(lb_ensemble *e, int nsteps) {
         const int rc = egraph(e, e->cur, &g);
         if (rc != LB_OK) return rc;
         LB_ETRY(e, "cudaGraphLaunch", cudaGraphLaunch(g, e->stream));
-        e->launches += 2L * e->graph_steps;
+        e->launches += (int64_t)launches_per_step(e) * e->graph_steps;
         rest -= e->graph_steps;
     }
     for (; rest > 0; rest--) {
@@ -391,8 +632,10 @@ int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy) {
 }
 
 int lb_ensemble_set_launch(lb_ensemble *e, int threads_x, int rows, int blocks_per_sm) {
-    if (!e || threads_x < 32 || threads_x % 32 || rows < 1 || threads_x * rows > 1024 ||
-        blocks_per_sm < 1 || blocks_per_sm > 32)
+    const bool tiles = threads_x == 0;
+    if (!e || blocks_per_sm < 1 || blocks_per_sm > 32 ||
+        (tiles && ens_tile_rows(rows) + ens_march_rows(rows) == 0) ||
+        (!tiles && (threads_x < 32 || threads_x % 32 || rows < 1 || threads_x * rows > 1024)))
         return LB_ERR_ARG;
     LB_ETRY(e, "lb_ensemble_set_launch", cudaStreamSynchronize(e->stream));
     e->shape = LaunchShape{threads_x, rows, blocks_per_sm};
@@ -411,33 +654,40 @@ int lb_ensemble_get_launch(const lb_ensemble *e, int out[3]) {
 // state.
 int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]) {
     if (!e || trial_steps < 1) return LB_ERR_ARG;
+    // the single-pass tiles, then the two-pass row groups {64, 128, 256
+    // threads} x {1, 2, 4 rows} x {2, 4, 8 blocks}
     static const int BX[3] = {64, 128, 256}, RY[3] = {1, 2, 4}, BPS[3] = {2, 4, 8};
-    float best = 1e30f;
-    LaunchShape pick = e->shape;
+    // (tile or strip shape, blocks per SM): each shape at its register-bound
+    // residency and at twice it
+    static const int TILES[14][2] = {{1, 5}, {1, 10}, {2, 6}, {2, 12}, {3, 2}, {3, 4}, {4, 3},
+                                     {5, 1}, {6, 3}, {6, 6}, {7, 4}, {7, 8}, {8, 3}, {9, 3}};
+    std::vector<LaunchShape> cand;
+    for (int k = 0; k < 14; k++) cand.push_back(LaunchShape{0, TILES[k][0], TILES[k][1]});
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
-            for (int k = 0; k < 3; k++) {
-                if (BX[i] * RY[j] > 512) continue;
-                int rc = lb_ensemble_set_launch(e, BX[i], RY[j], BPS[k]);
-                if (rc != LB_OK) return rc;
-                for (int s = 0; s < 1; s++) {
-                    LB_ETRY(e, "autotune", ens_step(e, e->cur, false));
-                    e->cur = 1 - e->cur;
-                }
-                LB_ETRY(e, "autotune", cudaEventRecord(e->ev0, e->stream));
-                for (int s = 0; s < trial_steps; s++) {
-                    LB_ETRY(e, "autotune", ens_step(e, e->cur, false));
-                    e->cur = 1 - e->cur;
-                }
-                LB_ETRY(e, "autotune", cudaEventRecord(e->ev1, e->stream));
-                LB_ETRY(e, "autotune", cudaEventSynchronize(e->ev1));
-                float ms = 0.f;
-                LB_ETRY(e, "autotune", cudaEventElapsedTime(&ms, e->ev0, e->ev1));
-                if (ms < best) {
-                    best = ms;
-                    pick = e->shape;
-                }
-            }
+            for (int k = 0; k < 3; k++)
+                if (BX[i] * RY[j] <= 512) cand.push_back(LaunchShape{BX[i], RY[j], BPS[k]});
+    float best = 1e30f;
+    LaunchShape pick = e->shape;
+    for (const LaunchShape &c : cand) {
+        int rc = lb_ensemble_set_launch(e, c.bx, c.ry, c.bps);
+        if (rc != LB_OK) return rc;
+        LB_ETRY(e, "autotune", ens_step(e, e->cur, false));  // one untimed step
+        e->cur = 1 - e->cur;
+        LB_ETRY(e, "autotune", cudaEventRecord(e->ev0, e->stream));
+        for (int s = 0; s < trial_steps; s++) {
+            LB_ETRY(e, "autotune", ens_step(e, e->cur, false));
+            e->cur = 1 - e->cur;
+        }
+        LB_ETRY(e, "autotune", cudaEventRecord(e->ev1, e->stream));
+        LB_ETRY(e, "autotune", cudaEventSynchronize(e->ev1));
+        float ms = 0.f;
+        LB_ETRY(e, "autotune", cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        if (ms < best) {
+            best = ms;
+            pick = e->shape;
+        }
+    }
     const int rc = lb_ensemble_set_launch(e, pick.bx, pick.ry, pick.bps);
     if (rc != LB_OK) return rc;
     if (out) lb_ensemble_get_launch(e, out);

@@ -36,9 +36,28 @@ def _single(pkg, n, G, rho, steps):
     return out
 
 
-@pytest.mark.parametrize("shape", [None, (64, 2, 2), (256, 1, 8)], ids=["default", "s64x2", "s256"])
-def test_ensemble_matches_single_domain_runs(pkg, shape):
-    nx, ny, G, rho = pkg.droplet_ensemble(5, seed=12, side_choices=[64, 96, 128, 160])
+@pytest.mark.parametrize("shape,sides", [
+    (None, [64, 96, 128, 160]),
+    ((64, 2, 2), [64, 96, 128, 160]),
+    ((256, 1, 8), [64, 96, 128, 160]),
+    ((0, 1, 2), [64, 96, 128, 160]),
+    ((0, 2, 6), [64, 96, 128, 160]),
+    ((0, 3, 2), [64, 96, 128, 160]),
+    ((0, 4, 3), [64, 96, 128, 160]),
+    ((0, 5, 1), [64, 96, 128, 160]),
+    ((0, 1, 5), [5, 9, 33, 37, 70]),      # tiles overhanging and wrapping small domains
+    ((0, 3, 2), [5, 9, 33, 37, 70]),
+    ((0, 5, 1), [5, 9, 17, 37, 70]),
+    ((0, 6, 3), [64, 96, 128, 160]),      # warps marching down 32-column strips
+    ((0, 7, 4), [64, 96, 128, 160]),
+    ((0, 8, 3), [5, 9, 33, 37, 70]),
+    ((0, 9, 3), [1, 2, 31, 40, 70]),
+    ((64, 1, 4), [5, 9, 33, 37, 70]),
+], ids=["default", "s64x2", "s256", "tiles1", "tiles2", "tiles3", "tiles4", "tiles5",
+        "tiles1-ragged", "tiles3-ragged", "tiles5-ragged", "march6", "march7",
+        "march8-ragged", "march9-ragged", "rows-ragged"])
+def test_ensemble_matches_single_domain_runs(pkg, shape, sides):
+    nx, ny, G, rho = pkg.droplet_ensemble(5, seed=12, side_choices=sides)
     ens = pkg.Ensemble(nx, ny, G)
     if shape:
         ens.set_launch(*shape)
@@ -47,7 +66,8 @@ def test_ensemble_matches_single_domain_runs(pkg, shape):
     ens.step(steps)
     f = ens.populations()
     mom = ens.moments()
-    assert ens.launches() >= 2 * steps
+    per_step = 2 if shape and shape[0] else 1  # two passes, or the single-pass tiles
+    assert ens.launches() >= per_step * steps
     for d in range(5):
         n = int(nx[d])
         fs, ms = _single(pkg, n, G[d], ens.domain(rho, d), steps)
@@ -65,7 +85,8 @@ def test_ensemble_autotune_keeps_results(pkg):
     ref.close()
     ens = pkg.Ensemble(nx, ny, G)
     shape = ens.autotune(trial_steps=2)
-    assert shape[0] in (64, 128, 256) and shape[1] in (1, 2, 4) and shape[2] in (2, 4, 8)
+    assert (shape[0] == 0 and 1 <= shape[1] <= 9 and 1 <= shape[2] <= 12) or \
+        (shape[0] in (64, 128, 256) and shape[1] in (1, 2, 4) and shape[2] in (2, 4, 8))
     ens.init_equilibrium(rho)  # tuning advanced the state: start over
     ens.step(40)
     assert beq(ens.populations(), f_ref)
