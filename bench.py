@@ -140,7 +140,11 @@ def run_ensemble(args, dist, ws, rank, local):
                                           seed=ENSEMBLE["seed"])
     steps = args.steps if args.steps else ENSEMBLE["steps"]
     ens = pkg.Ensemble(nx, ny, G)
-    shape = ens.autotune(trial_steps=3)
+    if args.launch_shape:
+        ens.set_launch(*args.launch_shape)
+        shape = list(args.launch_shape)
+    else:
+        shape = ens.autotune(trial_steps=3)
     ens.init_equilibrium(rho)
     ens.step(max(args.warmup, 3))
     if dist:
@@ -169,9 +173,11 @@ def run_ensemble(args, dist, ws, rank, local):
                        "total_nodes": NT, "sides": "multiples of 32 in [64, 512], seed %d"
                        % ENSEMBLE["seed"], "G": "U[-5.5,-4.5]", "tau": 1.0,
                        "psi": "1-exp(-rho)",
-                       "launch_shape": ({"single_pass_tiles": "32x%d" % {1: 8, 2: 8, 3: 16, 4: 16,
-                                                                         5: 32}[shape[1]],
-                                         "tile_shape": shape[1], "blocks_per_sm": shape[2]}
+                       "launch_shape": ({("single_pass_tiles" if shape[1] <= 5 else
+                                          "single_pass_warp_strips"):
+                                         "32x%d" % {1: 8, 2: 8, 3: 16, 4: 16, 5: 32, 6: 32,
+                                                    7: 32, 8: 64, 9: 16}[shape[1]],
+                                         "shape": shape[1], "blocks_per_sm": shape[2]}
                                         if shape[0] == 0 else
                                         {"threads_x": shape[0], "rows_per_item": shape[1],
                                          "blocks_per_sm": shape[2]}),
@@ -432,6 +438,9 @@ def main():
     ap.add_argument("--graph-steps", type=int, default=64)
     ap.add_argument("--domains", type=int, default=None,
                     help="ensemble: number of domains (profiling of a smaller case only)")
+    ap.add_argument("--launch-shape", type=int, nargs=3, default=None,
+                    metavar=("THREADS_X", "ROWS", "BLOCKS_PER_SM"),
+                    help="ensemble: this launch shape instead of the autotuner's pick")
     ap.add_argument("--size", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="other lattice extents (profiling of a smaller case only)")
     args = ap.parse_args()

@@ -273,11 +273,13 @@ int lb_ensemble_init_equilibrium(lb_ensemble *e, const float *rho);
 int lb_ensemble_step(lb_ensemble *e, int nsteps);  /* last step writes the moments */
 int lb_ensemble_time_steps(lb_ensemble *e, int nsteps, float *ms);
 int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy);
-/* launch shape.  threads_x = 0: one launch per step over tiles that form psi
- * of the tile and its ring in shared memory; rows then picks the tile shape
- * (1: 32 x 8 at 48 registers, the default with 5 blocks per SM; 2: 32 x 8 at
- * 40; 3: 32 x 16 at 60; 4: 32 x 16 at 40; 5: 32 x 32 at 60).  Otherwise the
- * two-pass step (psi pass, fused pass)
+/* launch shape.  threads_x = 0: one launch per step; rows then picks the
+ * form: 1..5 tiles that form psi of the tile and its ring in shared memory
+ * (1: 32 x 8 at 48 registers; 2: 32 x 8 at 40; 3: 32 x 16 at 60; 4: 32 x 16
+ * at 40; 5: 32 x 32 at 60), 6..9 warps marching down 32-column strips with
+ * psi of three rows in registers (6: 32 rows at 80 registers, the default
+ * with 3 blocks per SM; 7: 32 rows at 64; 8: 64 rows; 9: 16 rows).
+ * Otherwise the two-pass step (psi pass, fused pass)
  * over groups of `rows` rows with threads_x threads along x (a multiple of
  * 32).  Both give the same bits.  The autotuner times every candidate for
  * trial_steps steps on the ensemble itself (advancing its state: tune before

@@ -323,6 +323,25 @@ __device__ __forceinline__ void d2q9_bgk_native(float (&g)[9], float ux, float u
     pair(6, 8, a5, uy - ux);
 }
 
+// native Shan-Chen shift of (ex, ey): IF = sum_k w_k psi(x + c_k) c_k grouped
+// by the sign of each component (ps in the order psi(x), psi(x+1,y),
+// psi(x,row+1), psi(x-1,y), psi(x,row-1), then the diagonals (x+1,row+1),
+// (x-1,row+1), (x-1,row-1), (x+1,row-1); row+1 is physical -y), applied as
+// (-G psi(x)) inv_rt IF with inv_rt = 1/(tau_inv rho)
+__device__ __forceinline__ void d2q9_sc_shift_native(const float (&ps)[9], float w1, float w5,
+                                                     float G, float inv_rt, float &ex,
+                                                     float &ey) {
+    const float IFx = __fmaf_rn(w1, ps[1] - ps[3], w5 * ((ps[5] + ps[8]) - (ps[6] + ps[7])));
+    const float IFy = __fmaf_rn(w1, ps[4] - ps[2], w5 * ((ps[7] + ps[8]) - (ps[5] + ps[6])));
+    const float c = (-G * ps[0]) * inv_rt;
+    ex = __fmaf_rn(c, IFx, ex);
+    ey = __fmaf_rn(c, IFy, ey);
+}
+
+__device__ __forceinline__ float d2q9_rho_native(const float (&g)[9]) {
+    return (((g[1] + g[5]) + g[8]) + ((g[3] + g[6]) + g[7])) + ((g[0] + g[2]) + g[4]);
+}
+
 // native collision after the pull: moments, velocity-shift force with one
 // division 1/(rho tau_inv) (the form of reference src/collision.cu:280-284),
 // BGK; rho, ux, uy are the moments before the shift

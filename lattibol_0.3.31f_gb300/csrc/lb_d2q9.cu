@@ -88,12 +88,27 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
 #pragma unroll
         for (int k = 0; k < 9; k++) g[k] = ld_stream(a.src.f[k] + o + n.off(-d2_cx(k), -d2_cr(k)));
     }
-    if (MODE == MODE_NATIVE && !SC) {
+    if (MODE == MODE_NATIVE) {
+        // native arithmetic (d2q9_*_native); with Shan-Chen the pass stores
+        // psi, u_eq and the unrelaxed populations for the Shan-Chen pass
         float rho, ux, uy;
-        d2q9_collide_native(g, a.Fx, a.Fy, a.w0, a.w1, a.w5, a.tau_inv, rho, ux, uy);
+        if (!SC) {
+            d2q9_collide_native(g, a.Fx, a.Fy, a.w0, a.w1, a.w5, a.tau_inv, rho, ux, uy);
+            if (PLOT) a.plot[o] = make_float4(ux, uy, 0.f, rho);
+        } else {
+            d2q9_moments_native(g, rho, ux, uy);
+            float ex = ux, ey = uy;
+            if (a.Fx != 0.f || a.Fy != 0.f) {
+                const float inv_rt = 1.f / (rho * a.tau_inv);
+                if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+                if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            }
+            a.psi[o] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+            a.ueq_x[o] = ex;
+            a.ueq_y[o] = ey;
+        }
         if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
         if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
-        if (PLOT) a.plot[o] = make_float4(ux, uy, 0.f, rho);
 #pragma unroll
         for (int k = 0; k < 9; k++) a.dst.f[k][o] = g[k];
         return;
@@ -126,9 +141,28 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_fused_kernel(const D2Args a) {
 // ---------------------------------------------------------------------------
 // Shan-Chen force step, reference src/collision.cu:35-166: interaction force
 // -G psi(x) sum_k w_k psi(x + c_k) c_k and adhesion -G_ads psi(x) sum_k w_k
-// s(x + c_k) c_k shift u_eq, then BGK in place.  The accumulation order is the
-// reference's.  psi and the wall flags of the 3x3 stencil come through L1.
+// s(x + c_k) c_k shift u_eq, then BGK in place.  Reference mode: the
+// reference's accumulation order; native mode: d2q9_sc_shift_native, one
+// division and d2q9_bgk_native.  psi and the wall flags of the 3x3 stencil
+// come through L1.
 // ---------------------------------------------------------------------------
+// adhesion sums s = sum_k w_k [x + c_k is a wall] c_k in the reference's
+// order (src/collision.cu:105-140); m1..m8 are the stencil's node indices
+__device__ __forceinline__ void d2q9_adhesion_sums(const uint8_t *s, int m1, int m2, int m3,
+                                                   int m4, int m5, int m6, int m7, int m8,
+                                                   float w1, float w5, float &Fsx, float &Fsy) {
+    Fsx = 0.f;
+    Fsy = 0.f;
+    if (s[m1] & CELL_WALL) Fsx = Fsx + w1;
+    if (s[m2] & CELL_WALL) Fsy = Fsy - w1;
+    if (s[m3] & CELL_WALL) Fsx = Fsx - w1;
+    if (s[m4] & CELL_WALL) Fsy = Fsy + w1;
+    if (s[m5] & CELL_WALL) { Fsx = Fsx + w5; Fsy = Fsy - w5; }
+    if (s[m6] & CELL_WALL) { Fsx = Fsx - w5; Fsy = Fsy - w5; }
+    if (s[m7] & CELL_WALL) { Fsx = Fsx - w5; Fsy = Fsy + w5; }
+    if (s[m8] & CELL_WALL) { Fsx = Fsx + w5; Fsy = Fsy + w5; }
+}
+
 template <int MODE, bool PLOT>
 __global__ void __launch_bounds__(D2_BLOCK) d2q9_sc_kernel(const D2Args a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -148,18 +182,30 @@ __global__ void __launch_bounds__(D2_BLOCK) d2q9_sc_kernel(const D2Args a) {
                          __ldg(psi + m6),  __ldg(psi + m7), __ldg(psi + m8)};
     const float p0 = ps[0], rho = a.rho[o];
     float ex = a.ueq_x[o], ey = a.ueq_y[o];
+    if (MODE == MODE_NATIVE) {
+        // one division 1/(tau_inv rho) for the interaction and the adhesion
+        const float inv_rt = 1.f / (a.tau_inv * rho);
+        d2q9_sc_shift_native(ps, w1, w5, a.G, inv_rt, ex, ey);
+        if (a.Gads != 0.f) {
+            float Fsx, Fsy;
+            d2q9_adhesion_sums(a.flags, m1, m2, m3, m4, m5, m6, m7, m8, w1, w5, Fsx, Fsy);
+            const float c = (-a.Gads * p0) * inv_rt;
+            ex = __fmaf_rn(c, Fsx, ex);
+            ey = __fmaf_rn(c, Fsy, ey);
+        }
+        if (PLOT) a.plot[o] = make_float4(a.ux[o], a.uy[o], 0.f, rho);
+        float g[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) g[k] = a.dst.f[k][o];
+        d2q9_bgk_native(g, ex, ey, rho, a.w0, a.w1, a.w5, a.tau_inv);
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.dst.f[k][o] = g[k];
+        return;
+    }
     d2q9_sc_shift(ps, w1, w5, a.G, a.tau_inv, rho, ex, ey);
     if (a.Gads != 0.f) {
-        const uint8_t *s = a.flags;
-        float Fsx = 0.f, Fsy = 0.f;
-        if (s[m1] & CELL_WALL) Fsx = Fsx + w1;
-        if (s[m2] & CELL_WALL) Fsy = Fsy - w1;
-        if (s[m3] & CELL_WALL) Fsx = Fsx - w1;
-        if (s[m4] & CELL_WALL) Fsy = Fsy + w1;
-        if (s[m5] & CELL_WALL) { Fsx = Fsx + w5; Fsy = Fsy - w5; }
-        if (s[m6] & CELL_WALL) { Fsx = Fsx - w5; Fsy = Fsy - w5; }
-        if (s[m7] & CELL_WALL) { Fsx = Fsx - w5; Fsy = Fsy + w5; }
-        if (s[m8] & CELL_WALL) { Fsx = Fsx + w5; Fsy = Fsy + w5; }
+        float Fsx, Fsy;
+        d2q9_adhesion_sums(a.flags, m1, m2, m3, m4, m5, m6, m7, m8, w1, w5, Fsx, Fsy);
         Fsx = -a.Gads * p0 * Fsx;
         Fsy = -a.Gads * p0 * Fsy;
         ex = ex + (Fsx / (a.tau_inv * rho));

@@ -15,7 +15,8 @@
 // candidate on the ensemble itself.
 //
 // The per-node arithmetic is the single-domain native D2Q9 Shan-Chen step's
-// (same device functions, same order), so a domain of the ensemble evolves
+// (same device functions, same order: d2q9_moments_native,
+// d2q9_sc_shift_native, d2q9_bgk_native), so a domain of the ensemble evolves
 // bit for bit like the same domain run alone through the context API.
 #include <algorithm>
 #include <cstring>
@@ -82,8 +83,7 @@ __global__ void ens_density_kernel(const EnsArgs a) {
             for (int x = threadIdx.x; x < dm.W; x += blockDim.x) {
                 float g[9];
                 ens_pull(a, dm, x, y, g);
-                float rho, ux, uy;
-                d2q9_moments(g, rho, ux, uy);
+                const float rho = d2q9_rho_native(g);
                 a.psi[dm.off + x + dm.W * y] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
             }
         }
@@ -108,7 +108,7 @@ __global__ void ens_fused_kernel(const EnsArgs a) {
             float g[9];
             ens_pull(a, dm, x, y, g);
             float rho, ux, uy;
-            d2q9_moments(g, rho, ux, uy);
+            d2q9_moments_native(g, rho, ux, uy);
             const int xm = x == 0 ? dm.W - 1 : x - 1, xp = x == dm.W - 1 ? 0 : x + 1;
             const int W = dm.W;
             const float ps[9] = {__ldg(psi + x + W * y),   __ldg(psi + xp + W * y),
@@ -117,8 +117,8 @@ __global__ void ens_fused_kernel(const EnsArgs a) {
                                  __ldg(psi + xm + W * rp), __ldg(psi + xm + W * rm),
                                  __ldg(psi + xp + W * rm)};
             float ex = ux, ey = uy;
-            d2q9_sc_shift(ps, a.w1, a.w5, dm.G, dm.tau_inv, rho, ex, ey);
-            d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, dm.tau_inv);
+            d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rho), ex, ey);
+            d2q9_bgk_native(g, ex, ey, rho, a.w0, a.w1, a.w5, dm.tau_inv);
             const int o = dm.off + x + W * y;
             if (MOM) { a.rho[o] = rho; a.ux[o] = ux; a.uy[o] = uy; }
 #pragma unroll
@@ -186,11 +186,10 @@ __global__ void __launch_bounds__(ET_BX * BY, MINB) ens_tile_kernel(const EnsArg
             ens_pull(a, dm, ens_wrap(dm.x - 1 + rx, dm.W, small),
                      ens_wrap(dm.y - 1 + ry, dm.H, small), g2);
         float rho, ux, uy;
-        d2q9_moments(g, rho, ux, uy);
+        d2q9_moments_native(g, rho, ux, uy);
         sp[ty + 1][tx + 1] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
         if (ring) {
-            float r2, u2, v2;
-            d2q9_moments(g2, r2, u2, v2);
+            const float r2 = d2q9_rho_native(g2);
             sp[ry][rx] = a.psi_form == 0 ? psi_ref(r2) : psi_exp1(r2);
         }
         __syncthreads();
@@ -201,8 +200,8 @@ __global__ void __launch_bounds__(ET_BX * BY, MINB) ens_tile_kernel(const EnsArg
                                  sp[ty + 1][tx],     sp[ty][tx + 1],     sp[ty + 2][tx + 2],
                                  sp[ty + 2][tx],     sp[ty][tx],         sp[ty][tx + 2]};
             float ex = ux, ey = uy;
-            d2q9_sc_shift(ps, a.w1, a.w5, dm.G, dm.tau_inv, rho, ex, ey);
-            d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, dm.tau_inv);
+            d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rho), ex, ey);
+            d2q9_bgk_native(g, ex, ey, rho, a.w0, a.w1, a.w5, dm.tau_inv);
             const int o = dm.off + xt + dm.W * yt;
             if (MOM) { a.rho[o] = rho; a.ux[o] = ux; a.uy[o] = uy; }
 #pragma unroll
@@ -245,21 +244,18 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(cons
         float gc[9], rc, uxc, uyc;  // row r: pulled populations and moments at x
         float pm, pc, hm = 0.f, hc = 0.f;  // psi of rows r - 1, r (h: the halo column)
         {
-            float g[9], r0, u0, v0;
+            float g[9];
             const int ym = ens_wrap(dm.y - 1, dm.H, false);
             ens_pull(a, dm, x, ym, g);
-            d2q9_moments(g, r0, u0, v0);
-            pm = ens_psi(a, r0);
+            pm = ens_psi(a, d2q9_rho_native(g));
             ens_pull(a, dm, x, dm.y, gc);
-            d2q9_moments(gc, rc, uxc, uyc);
+            d2q9_moments_native(gc, rc, uxc, uyc);
             pc = ens_psi(a, rc);
             if (edge) {
                 ens_pull(a, dm, xh, ym, g);
-                d2q9_moments(g, r0, u0, v0);
-                hm = ens_psi(a, r0);
+                hm = ens_psi(a, d2q9_rho_native(g));
                 ens_pull(a, dm, xh, dm.y, g);
-                d2q9_moments(g, r0, u0, v0);
-                hc = ens_psi(a, r0);
+                hc = ens_psi(a, d2q9_rho_native(g));
             }
         }
         for (int r = dm.y; r < y_end; r++) {
@@ -267,12 +263,11 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(cons
             float gn[9], rn, uxn, uyn, hn = 0.f;
             ens_pull(a, dm, x, yp, gn);
             if (edge) {
-                float g[9], r0, u0, v0;
+                float g[9];
                 ens_pull(a, dm, xh, yp, g);
-                d2q9_moments(g, r0, u0, v0);
-                hn = ens_psi(a, r0);
+                hn = ens_psi(a, d2q9_rho_native(g));
             }
-            d2q9_moments(gn, rn, uxn, uyn);
+            d2q9_moments_native(gn, rn, uxn, uyn);
             const float pn = ens_psi(a, rn);
             // x - 1 and x + 1 from the neighbour lanes, the halo at the strip ends
             float lm = __shfl_up_sync(FULL, pm, 1), lc = __shfl_up_sync(FULL, pc, 1);
@@ -286,8 +281,8 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(cons
                 // psi(x-1,y), psi(x,row-1), then the diagonals
                 const float ps[9] = {pc, qc, pn, lc, pm, qn, ln, lm, qm};
                 float ex = uxc, ey = uyc;
-                d2q9_sc_shift(ps, a.w1, a.w5, dm.G, dm.tau_inv, rc, ex, ey);
-                d2q9_bgk(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
+                d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rc), ex, ey);
+                d2q9_bgk_native(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
                 const int o = dm.off + x + dm.W * r;
                 if (MOM) { a.rho[o] = rc; a.ux[o] = uxc; a.uy[o] = uyc; }
 #pragma unroll
@@ -352,7 +347,7 @@ struct lb_ensemble {
     EnsItem *items_d = nullptr;
     int nitems = 0, items_cap = 0;
     int cur = 0, psi_form = LB_PSI_EXP1, sms = 1, graph_steps = 32;
-    LaunchShape shape{0, 1, 5};  // single-pass 32 x 8 tiles, 5 blocks per SM (48 registers)
+    LaunchShape shape{0, 6, 3};  // single-pass warp strips of 32 rows, 3 blocks per SM
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};

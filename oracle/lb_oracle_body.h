@@ -363,6 +363,54 @@ static void FN(d2q9_sc_pass)(float *plot, R *f, const uint8_t *solid, const R *u
     }
 }
 
+/* The Shan-Chen pass in native mode (lattibol_0.3.31f_gb300/csrc/lb_d2q9.cu,
+ * d2q9_sc_kernel<MODE_NATIVE>): the stencil sums grouped by sign
+ * (d2q9_sc_shift_native), one division 1/(tau_inv rho) shared by the
+ * interaction and the adhesion, FMA shifts, the native BGK. */
+static void FN(d2q9_sc_pass_native)(R *f, const uint8_t *solid, const R *rho, const R *psi,
+                                    const R *ueq_x, const R *ueq_y, int W, int H, R w0, R w1,
+                                    R w5, R tau_inv, R G, R Gads)
+{
+    const long N = (long)W * H;
+#pragma omp parallel for schedule(static)
+    for (long o = 0; o < N; o++) {
+        if (solid[o]) continue;
+        const int x = (int)(o % W), y = (int)(o / W);
+        const int xn = x > 0 ? x - 1 : W - 1, xp = x < W - 1 ? x + 1 : 0;
+        const int yn = y > 0 ? y - 1 : H - 1, yp = y < H - 1 ? y + 1 : 0;
+        long m[9];
+        m[0] = (long)y * W + x;   m[1] = (long)y * W + xp;  m[2] = (long)yp * W + x;
+        m[3] = (long)y * W + xn;  m[4] = (long)yn * W + x;  m[5] = (long)yp * W + xp;
+        m[6] = (long)yp * W + xn; m[7] = (long)yn * W + xn; m[8] = (long)yn * W + xp;
+        R ps[9];
+        for (int k = 0; k < 9; k++) ps[k] = psi[m[k]];
+        const R IFx = FMA_R(w1, ps[1] - ps[3], w5 * ((ps[5] + ps[8]) - (ps[6] + ps[7])));
+        const R IFy = FMA_R(w1, ps[4] - ps[2], w5 * ((ps[7] + ps[8]) - (ps[5] + ps[6])));
+        const R inv_rt = (R)1 / (tau_inv * rho[o]);
+        const R c = (-G * ps[0]) * inv_rt;
+        R vx = FMA_R(c, IFx, ueq_x[o]);
+        R vy = FMA_R(c, IFy, ueq_y[o]);
+        if (Gads != 0) {
+            R Fsx = 0, Fsy = 0;
+            if (solid[m[1]]) Fsx = Fsx + w1;
+            if (solid[m[2]]) Fsy = Fsy - w1;
+            if (solid[m[3]]) Fsx = Fsx - w1;
+            if (solid[m[4]]) Fsy = Fsy + w1;
+            if (solid[m[5]]) { Fsx = Fsx + w5; Fsy = Fsy - w5; }
+            if (solid[m[6]]) { Fsx = Fsx - w5; Fsy = Fsy - w5; }
+            if (solid[m[7]]) { Fsx = Fsx - w5; Fsy = Fsy + w5; }
+            if (solid[m[8]]) { Fsx = Fsx + w5; Fsy = Fsy + w5; }
+            const R ca = (-Gads * ps[0]) * inv_rt;
+            vx = FMA_R(ca, Fsx, vx);
+            vy = FMA_R(ca, Fsy, vy);
+        }
+        R g[9];
+        for (int k = 0; k < 9; k++) g[k] = f[k * N + o];
+        FN(d2q9_bgk_native)(g, vx, vy, rho[o], w0, w1, w5, tau_inv);
+        for (int k = 0; k < 9; k++) f[k * N + o] = g[k];
+    }
+}
+
 /* Collision launcher, src/collision.cu:168-355: first kernel (local swap,
  * Zou-He west inlet / east outlet, moments, force shift, BGK or -- if G != 0 --
  * psi/u_eq output without relaxation), then the Shan-Chen pass when G < 0. */
@@ -546,11 +594,11 @@ void FN(lbo_d2q9_stream_native)(R *f, const uint8_t *flags, const R *corr, int W
         }
 }
 
-/* Native D2Q9 collision.  Without Shan-Chen: the native arithmetic
- * (d2q9_moments_native, d2q9_bgk_native).  With it: the reference's two-pass
- * structure (moments, psi, u_eq; then the Shan-Chen pass) without Zou-He,
- * with psi defined (0) at wall cells, the psi form selectable, and the
- * interaction applied for any G != 0. */
+/* Native D2Q9 collision, in the native arithmetic (d2q9_moments_native,
+ * d2q9_bgk_native).  With Shan-Chen: the reference's two-pass structure
+ * (moments, psi, u_eq; then the Shan-Chen pass, d2q9_sc_pass_native) without
+ * Zou-He, with psi defined (0) at wall cells, the psi form selectable, and
+ * the interaction applied for any G != 0. */
 void FN(lbo_d2q9_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *rho, R *psi,
                                  int W, int H, R w0, R w1, R w5, R tau_inv, R Fx, R Fy, R G,
                                  R Gads, int psi_form)
@@ -595,22 +643,23 @@ void FN(lbo_d2q9_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *rh
             for (int k = 0; k < 9; k++) f[k * N + o] = g[k];
             continue;
         }
-        FN(d2q9_moments)(g, &r, &vx, &vy);
+        /* with Shan-Chen: the native moments and force shift, then psi and
+         * u_eq for the native Shan-Chen pass */
+        FN(d2q9_moments_native)(g, &r, &vx, &vy);
         R ex = vx, ey = vy;
-        if (Fx != 0) ex = vx + Fx / (r * tau_inv);
-        if (Fy != 0) ey = vy + Fy / (r * tau_inv);
-        if (rho) { ux[o] = vx; uy[o] = vy; rho[o] = r; }
-        if (sc) {
-            psi[o] = FN(psi_of)(r, psi_form);
-            r_buf[o] = r; ex_buf[o] = ex; ey_buf[o] = ey;
-        } else {
-            FN(d2q9_bgk)(g, ex, ey, r, w0, w1, w5, tau_inv);
+        if (Fx != 0 || Fy != 0) {
+            const R inv_rt = (R)1 / (r * tau_inv);
+            if (Fx != 0) ex = FMA_R(Fx, inv_rt, vx);
+            if (Fy != 0) ey = FMA_R(Fy, inv_rt, vy);
         }
+        if (rho) { ux[o] = vx; uy[o] = vy; rho[o] = r; }
+        psi[o] = FN(psi_of)(r, psi_form);
+        r_buf[o] = r; ex_buf[o] = ex; ey_buf[o] = ey;
         for (int k = 0; k < 9; k++) f[k * N + o] = g[k];
     }
     if (sc) {
-        FN(d2q9_sc_pass)(NULL, f, solid, r_buf /*unused*/, r_buf /*unused*/, r_buf, psi,
-                         ex_buf, ey_buf, W, H, w0, w1, w5, tau_inv, G, Gads);
+        FN(d2q9_sc_pass_native)(f, solid, r_buf, psi, ex_buf, ey_buf, W, H, w0, w1, w5, tau_inv,
+                                G, Gads);
         free(ex_buf); free(ey_buf); free(r_buf); free(solid);
     }
 }
