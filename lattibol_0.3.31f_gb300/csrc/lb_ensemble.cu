@@ -654,10 +654,10 @@ int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]) {
     static const int BX[3] = {64, 128, 256}, RY[3] = {1, 2, 4}, BPS[3] = {2, 4, 8};
     // (tile or strip shape, blocks per SM): each shape at its register-bound
     // residency and at twice it
-    static const int TILES[14][2] = {{1, 5}, {1, 10}, {2, 6}, {2, 12}, {3, 2}, {3, 4}, {4, 3},
-                                     {5, 1}, {6, 3}, {6, 6}, {7, 4}, {7, 8}, {8, 3}, {9, 3}};
+    static const int TILES[][2] = {{1, 5}, {1, 10}, {2, 6}, {2, 12}, {3, 2}, {3, 4}, {4, 3},
+                                   {5, 1}, {6, 3}, {6, 6}, {7, 4}, {7, 8}, {8, 3}, {9, 3}};
     std::vector<LaunchShape> cand;
-    for (int k = 0; k < 14; k++) cand.push_back(LaunchShape{0, TILES[k][0], TILES[k][1]});
+    for (const auto &t : TILES) cand.push_back(LaunchShape{0, t[0], t[1]});
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
             for (int k = 0; k < 3; k++)
