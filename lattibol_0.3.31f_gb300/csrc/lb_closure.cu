@@ -33,35 +33,56 @@ using namespace lb;
 namespace lb {
 
 // ------------------------------------------------------------------ features
-// raw moment polynomials of the 18 non-conserved features
+// The 18 raw non-equilibrium moments sum_k P(c_k) (g_k - feq_k) as raw
+// moments of g minus the moments of the D3Q19 second-order equilibrium in
+// closed form (exact identities of the lattice: sum c_a feq = rho u_a,
+// sum c_a^2 feq = rho/3 + rho u_a^2, sum c_a c_b feq = rho u_a u_b,
+// sum c_a c_b^2 feq = rho u_a / 3, sum c_a^2 c_b^2 feq = rho (1/9 - u^2/6 +
+// (u_a^2 + u_b^2)/2)).  The raw moments come from the four edge velocities of
+// each coordinate plane: with g_pp, g_pm, g_mp, g_mm the plane's (+,+), (+,-),
+// (-,+), (-,-) populations, sum c_a c_b = (pp + mm) - (pm + mp), sum c_a c_b^2
+// = (pp + pm) - (mp + mm) (also the plane's part of sum c_a), sum c_b c_a^2 =
+// (pp + mp) - (pm + mm), sum c_a^2 c_b^2 = (pp + pm) + (mp + mm).
+struct PlaneSums {
+    float ab, a_b2, b_a2, a2b2;
+    __device__ __forceinline__ PlaneSums(float pp, float pm, float mp, float mm) {
+        ab = (pp + mm) - (pm + mp);
+        a_b2 = (pp + pm) - (mp + mm);
+        b_a2 = (pp + mp) - (pm + mm);
+        a2b2 = (pp + pm) + (mp + mm);
+    }
+};
+
 __device__ __forceinline__ void closure_features(const float (&g)[19], float rho, float ux,
                                                  float uy, float uz, float tau0, float s_ref,
                                                  float (&feat)[MLP_IN]) {
-    // the lattice coefficients are 0 or +-1 and known at compile time after
-    // unrolling; terms with a zero coefficient are skipped explicitly (a float
-    // multiply by 0 could not be folded away)
+    // planes (a, b): xy = (7, 8, 11, 12), xz = (9, 10, 13, 14), yz = (15, 16, 17, 18)
+    const PlaneSums xy(g[7], g[8], g[11], g[12]);
+    const PlaneSums xz(g[9], g[10], g[13], g[14]);
+    const PlaneSums yz(g[15], g[16], g[17], g[18]);
+    const float third = 1.f / 3.f;
+    const float rx = rho * ux, ry = rho * uy, rz = rho * uz;
+    const float uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+    const float e4 = 1.f / 9.f - (uxx + uyy + uzz) * (1.f / 6.f);
     float m[18];
-#pragma unroll
-    for (int i = 0; i < 18; i++) m[i] = 0.f;
-    const float usq = ux * ux + uy * uy + uz * uz;
-    auto addc = [](float acc, int c, float v) { return c > 0 ? acc + v : (c < 0 ? acc - v : acc); };
-#pragma unroll
-    for (int k = 0; k < 19; k++) {
-        const int cx = d3_cx(k), cy = d3_cy(k), cz = d3_cz(k);
-        const float wk = k == 0 ? 1.f / 3.f : (k < 7 ? 1.f / 18.f : 1.f / 36.f);
-        const float cu = addc(addc(addc(0.f, cx, ux), cy, uy), cz, uz);
-        const float feq = wk * rho * (1.f + 3.f * cu + 4.5f * cu * cu - 1.5f * usq);
-        const float fn = g[k] - feq;
-        m[0] = addc(m[0], cx, fn);  m[1] = addc(m[1], cy, fn);  m[2] = addc(m[2], cz, fn);
-        m[3] = addc(m[3], cx * cx, fn);  m[4] = addc(m[4], cy * cy, fn);
-        m[5] = addc(m[5], cz * cz, fn);  m[6] = addc(m[6], cx * cy, fn);
-        m[7] = addc(m[7], cx * cz, fn);  m[8] = addc(m[8], cy * cz, fn);
-        m[9] = addc(m[9], cx * cy * cy, fn);   m[10] = addc(m[10], cx * cz * cz, fn);
-        m[11] = addc(m[11], cy * cx * cx, fn); m[12] = addc(m[12], cy * cz * cz, fn);
-        m[13] = addc(m[13], cz * cx * cx, fn); m[14] = addc(m[14], cz * cy * cy, fn);
-        m[15] = addc(m[15], cx * cx * cy * cy, fn); m[16] = addc(m[16], cx * cx * cz * cz, fn);
-        m[17] = addc(m[17], cy * cy * cz * cz, fn);
-    }
+    m[0] = ((g[1] - g[2]) + (xy.a_b2 + xz.a_b2)) - rx;
+    m[1] = ((g[3] - g[4]) + (xy.b_a2 + yz.a_b2)) - ry;
+    m[2] = ((g[5] - g[6]) + (xz.b_a2 + yz.b_a2)) - rz;
+    m[3] = ((g[1] + g[2]) + (xy.a2b2 + xz.a2b2)) - (rho * third + rx * ux);
+    m[4] = ((g[3] + g[4]) + (xy.a2b2 + yz.a2b2)) - (rho * third + ry * uy);
+    m[5] = ((g[5] + g[6]) + (xz.a2b2 + yz.a2b2)) - (rho * third + rz * uz);
+    m[6] = xy.ab - rx * uy;
+    m[7] = xz.ab - rx * uz;
+    m[8] = yz.ab - ry * uz;
+    m[9] = xy.a_b2 - rx * third;
+    m[10] = xz.a_b2 - rx * third;
+    m[11] = xy.b_a2 - ry * third;
+    m[12] = yz.a_b2 - ry * third;
+    m[13] = xz.b_a2 - rz * third;
+    m[14] = yz.b_a2 - rz * third;
+    m[15] = xy.a2b2 - rho * (e4 + 0.5f * (uxx + uyy));
+    m[16] = xz.a2b2 - rho * (e4 + 0.5f * (uxx + uzz));
+    m[17] = yz.a2b2 - rho * (e4 + 0.5f * (uyy + uzz));
     const float scale = 1.f / (rho * (1.f / 3.f) * tau0 * s_ref);
 #pragma unroll
     for (int i = 0; i < 18; i++) feat[i] = m[i] * scale;
@@ -149,9 +170,12 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
 //   3. each warp loads its 32 lanes of D, adds b1, applies ReLU and writes the
 //      BF16 hidden row over A (now K = 64);
 //   4. thread 0 issues D = H W2^T (four k16 MMAs) into the same columns;
-//   5. each thread loads its row, adds b2, applies ReLU and sums w3 h + b3.
+//   5. each thread loads its row, adds b2, applies ReLU and sums w3 h + b3
+//      (fused multiply-adds).
 // Rounding points are the warp-level kernel's (BF16 inputs, weights and
-// first hidden layer; FP32 accumulation, biases and last layer).
+// first hidden layer; FP32 accumulation, biases and last layer) except that
+// the last layer's products are fused into the sum (one rounding each, not
+// two).
 // ---------------------------------------------------------------------------
 constexpr int TC_COLS = 64;             // tensor-memory columns per block (D is 128 x 64)
 constexpr int TC_WAIT = 1 << 22;        // mbarrier polls before a block gives up
@@ -285,7 +309,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
             tc_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
             for (int j = 0; j < 32; j++)
-                yv = yv + ca.head_w3[c + j] * fmaxf(v[j] + ca.head_b2[c + j], 0.f);
+                yv = __fmaf_rn(ca.head_w3[c + j], fmaxf(v[j] + ca.head_b2[c + j], 0.f), yv);
         }
         yv = yv + ca.head_b3;
         tc_fence_before();  // the next run's MMA overwrites these columns after a barrier
