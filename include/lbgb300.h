@@ -167,7 +167,7 @@ typedef enum {
 #define LB_TUNE_SC_SINGLE_PASS 0x002 /* D3Q19 Shan-Chen: the single-pass z-marching
                                         kernel (psi halo in shared memory) instead of
                                         the separate psi pass; same results, measured
-                                        slower (17.7 vs 25.9 GLUPS at 256^3) */
+                                        slower (24.8 vs 26.3 GLUPS FP32 at 256^3) */
 #define LB_TUNE_PERSISTENT 0x004 /* D2Q9 without Shan-Chen: lb_step runs all its steps
                                     in one cooperative launch whose blocks own row
                                     bands and wait (bounded) only for their two

@@ -136,14 +136,19 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a)
 
 // ---------------------------------------------------------------------------
 // Single-pass Shan-Chen step.  A block owns a SC_TX x SC_TY column tile and
-// marches through a chunk of SC_ZC planes.  For every plane it pulls the
-// populations of its 256 nodes and of the 84-node ring around them, keeps
-// psi of three consecutive planes (with that halo) in shared memory and the
-// pulled populations of the next plane in registers; a plane is relaxed once
-// psi of the plane above is known.  Each population is read from DRAM once
-// per step (the halo pulls are L2 hits) and psi never leaves the SM.  The
-// arithmetic is the two-pass path's (same pulls, rho sum, stencil order), so
-// both produce the same bits.
+// marches through a chunk of planes.  For plane z + 1 it pulls the
+// populations of its 256 nodes (kept in shared memory, each thread's own
+// column of a plane buffer) and of the 84-node ring around them and writes
+// their psi into one of four plane slots; after one barrier it relaxes plane
+// z from the populations it kept one plane earlier and the psi stencil of
+// planes z - 1, z, z + 1.  DRAM sees each population once per step and psi
+// never leaves the SM.  Four psi slots make one barrier per plane enough: a
+// warp writing the slot of plane z + 2 has passed the barrier of plane z + 1,
+// which every warp reaches only after relaxing plane z - 1, the last reader of
+// that slot; the population buffers are private to their thread.  Keeping
+// the populations in shared memory rather than registers holds the kernel at
+// 64 registers (4 blocks per SM).  The arithmetic is the two-pass path's
+// (same pulls, rho sum, stencil order), so both produce the same bits.
 // ---------------------------------------------------------------------------
 constexpr int SC_TX = 32, SC_TY = 8, SC_HX = SC_TX + 2, SC_HY = SC_TY + 2;
 constexpr int SC_THREADS = SC_TX * SC_TY;            // 256
@@ -162,8 +167,9 @@ __device__ __forceinline__ float sc_psi_of_node(const D3Args &a, int x, int y, i
 }
 
 template <typename S, bool MOM>
-__global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args a, int zc) {
-    __shared__ float sp[3][SC_HY][SC_HX];
+__global__ void __launch_bounds__(SC_THREADS, 4) d3q19_sc_march_kernel(const D3Args a, int zc) {
+    __shared__ float sp[4][SC_HY][SC_HX];
+    __shared__ float sg[2][19][SC_THREADS];  // pulled populations of planes z, z + 1
     const int tid = threadIdx.x, tx = tid % SC_TX, ty = tid / SC_TX;
     const int x0 = blockIdx.x * SC_TX, y0 = blockIdx.y * SC_TY, z0 = blockIdx.z * zc;
     const int x = x0 + tx, y = y0 + ty;
@@ -178,40 +184,40 @@ __global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args
         hy = (tid - 2 * SC_HX) % SC_TY;
     }
     const int hxg = (x0 + hx + a.W) % a.W, hyg = (y0 + hy + a.H) % a.H;
-
-    float g_cur[19], g_next[19];
-    uint8_t fl_cur = 0, fl_next = 0;
-    // psi (and, for the own node, the populations) of plane zl into ring slot s
-    auto load_plane = [&](int zl, int s, bool keep) {
+    // psi of plane zl (own node and ring node) into its slot; the own node's
+    // pulled populations into buffer zl & 1
+    auto psi_plane = [&](int zl) {
         const int zz = (zl % a.D + a.D) % a.D;
+        const int s = (zl + 4) & 3;
         const int o = x + a.W * (y + a.H * zz);
         const uint8_t fl = a.flags[o];
         float psi = 0.f;
         if (!(fl & CELL_WALL)) {
+            float g[19];
             const Nbr3 n(x, y, zz, a.W, a.H, a.D);
-            pull_native<S>(a, o, n, fl, g_next);
-            const float rho = d3q19_rho_native(g_next);
+            pull_native<S>(a, o, n, fl, g);
+            const float rho = d3q19_rho_native(g);
             psi = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+#pragma unroll
+            for (int k = 0; k < 19; k++) sg[zl & 1][k][tid] = g[k];
         }
-        if (keep) fl_next = fl;
         sp[s][ty + 1][tx + 1] = psi;
         if (tid < SC_HALO) sp[s][hy + 1][hx + 1] = sc_psi_of_node<S>(a, hxg, hyg, zz);
     };
 
-    load_plane(z0 - 1, 0, false);
-    load_plane(z0, 1, true);
-#pragma unroll
-    for (int k = 0; k < 19; k++) g_cur[k] = g_next[k];
-    fl_cur = fl_next;
+    psi_plane(z0 - 1);
+    psi_plane(z0);
     for (int z = z0; z < z0 + zc; z++) {
-        const int r = z - z0 + 1;  // ring index of plane z
-        __syncthreads();           // slot (r+1)%3 held plane z-2, read by the last iteration
-        load_plane(z + 1, (r + 1) % 3, true);
+        psi_plane(z + 1);
         __syncthreads();
-        if (!(fl_cur & CELL_WALL)) {
-            const int o = x + a.W * (y + a.H * z);
+        const int o = x + a.W * (y + a.H * z);
+        const uint8_t fl = a.flags[o];
+        if (!(fl & CELL_WALL)) {
+            float g[19];
+#pragma unroll
+            for (int k = 0; k < 19; k++) g[k] = sg[z & 1][k][tid];
             float rho, ux, uy, uz;
-            d3q19_moments_native(g_cur, rho, ux, uy, uz);
+            d3q19_moments_native(g, rho, ux, uy, uz);
             if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
             if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
             const float inv_rt = 1.f / (rho * a.tau_inv);
@@ -222,34 +228,36 @@ __global__ void __launch_bounds__(SC_THREADS) d3q19_sc_march_kernel(const D3Args
             float ps[19];
 #pragma unroll
             for (int k = 0; k < 19; k++)
-                ps[k] = sp[(r + d3_cz(k) + 3) % 3][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
+                ps[k] = sp[(z + d3_cz(k) + 4) & 3][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
             float IFx, IFy, IFz;
             d3q19_sc_sum_native(ps, a.w1, a.w7, IFx, IFy, IFz);
             const float c = (-a.G * ps[0]) * inv_rt;
             ex = __fmaf_rn(c, IFx, ex);
             ey = __fmaf_rn(c, IFy, ey);
             ez = __fmaf_rn(c, IFz, ez);
-            d3q19_bgk_native(g_cur, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+            d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
             S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
-            for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g_cur[k], a.wr[k]);
+            for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], a.wr[k]);
         } else {
-            const int o = x + a.W * (y + a.H * z);
             if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
             if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-#pragma unroll
-        for (int k = 0; k < 19; k++) g_cur[k] = g_next[k];
-        fl_cur = fl_next;
     }
 }
 
-// z-chunk of the marching kernel for a lattice, 0 if the shape does not tile
+// z-chunk of the marching kernel for a lattice, 0 if the shape does not tile:
+// the longest march that still gives at least 1216 blocks (two waves of 4
+// blocks on 152 SMs), else the shortest
 int sc_march_chunk(int W, int H, int D) {
     if (W % SC_TX || H % SC_TY) return 0;
-    for (int zc : {32, 16, 8})
-        if (D % zc == 0) return zc;
-    return 0;
+    int pick = 0;
+    for (int zc : {32, 16, 8}) {
+        if (D % zc) continue;
+        pick = zc;
+        if ((long)(W / SC_TX) * (H / SC_TY) * (D / zc) >= 1216) return zc;
+    }
+    return pick;
 }
 
 template <typename S>
