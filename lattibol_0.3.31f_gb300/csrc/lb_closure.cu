@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
 //      (K-major 8x8 core matrices, lb_tc05.cuh);
 //   2. thread 0 issues D = A W1^T (M 128, N 64, two k16 MMAs, FP32 in 64
 //      tensor-memory columns) and commits to an mbarrier;
-//   3. each warp loads its 32 lanes of D, adds b1, applies ReLU and writes the
-//      BF16 hidden row over A (now K = 64);
+//   3. each warp loads its 32 lanes of D, adds b1 and writes the hidden row,
+//      ReLU and BF16 rounding in one conversion, over A (now K = 64);
 //   4. thread 0 issues D = H W2^T (four k16 MMAs) into the same columns;
 //   5. each thread loads its row, adds b2, applies ReLU and sums w3 h + b3
 //      (fused multiply-adds).
@@ -177,6 +177,14 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
 // the last layer's products are fused into the sum (one rounding each, not
 // two).
 // ---------------------------------------------------------------------------
+// ReLU and round-to-nearest BF16 of two floats in one conversion, lo in the
+// low half (the PTX packs its first source into the high half)
+__device__ __forceinline__ uint32_t bf16x2_relu(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
 constexpr int TC_COLS = 64;             // tensor-memory columns per block (D is 128 x 64)
 constexpr int TC_WAIT = 1 << 22;        // mbarrier polls before a block gives up
 
@@ -274,15 +282,14 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
             tc_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
             for (int h = 0; h < 4; h++) {
-                __nv_bfloat162 p[4];
+                uint32_t p[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int q = 8 * h + 2 * j;
-                    p[j] = __floats2bfloat162_rn(fmaxf(v[q] + ca.head_b1[c + q], 0.f),
-                                                 fmaxf(v[q + 1] + ca.head_b1[c + q + 1], 0.f));
+                    p[j] = bf16x2_relu(v[q] + ca.head_b1[c + q], v[q + 1] + ca.head_b1[c + q + 1]);
                 }
                 *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, c + 8 * h, MLP_H)) =
-                    *reinterpret_cast<const uint4 *>(p);
+                    make_uint4(p[0], p[1], p[2], p[3]);
             }
         }
         fence_proxy_async();
