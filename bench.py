@@ -361,7 +361,7 @@ def dist_max(dist, v):
     return float(t.item())
 
 
-def cpu_baseline(wl, budget_s=15.0, max_steps=None):
+def cpu_baseline(wl, budget_s=15.0, max_steps=None, warmup=0):
     """The oracle's float port of the reference loop (swap streaming + collision,
     native boundary mode) on the workload's full lattice with all host threads,
     timed for a bounded number of steps."""
@@ -389,6 +389,8 @@ def cpu_baseline(wl, budget_s=15.0, max_steps=None):
     steps = 0
     t0 = time.perf_counter()
     while True:
+        if warmup and steps == warmup:
+            steps, warmup, t0 = 0, 0, time.perf_counter()  # untimed warm-up done
         if wl.lattice == 19:
             orc.d3q19_stream_native(f, flags, corr, nx, ny, nz)
             orc.d3q19_collide_native(f, flags, None, nx, ny, nz, *w, tau_inv, F, G=wl.G, psi=psi)
@@ -397,7 +399,7 @@ def cpu_baseline(wl, budget_s=15.0, max_steps=None):
             orc.d2q9_collide_native(f, flags, None, nx, ny, *w, tau_inv, F[:2])
         steps += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or (max_steps and steps >= max_steps):
+        if not warmup and (el >= budget_s or (max_steps and steps >= max_steps)):
             break
     return {"value": N * steps / el / 1e9, "unit": "GLUPS", "cores": orc.num_threads(),
             "kind": "port", "steps": steps, "seconds": el,
@@ -410,9 +412,9 @@ def run_reference(args, wl):
     if rank != 0:
         return 0
     budget = float(os.environ.get("LB_CPU_BUDGET_S", "60"))
-    cb = cpu_baseline(wl, budget_s=budget, max_steps=args.steps)
+    cb = cpu_baseline(wl, budget_s=budget, max_steps=args.steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": "GLUPS", "value": cb["value"], "unit": "GLUPS",
-            "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 0,
+            "n_gpus": args.gpus, "steps": cb["steps"], "warmup": args.warmup,
             "ms_per_step": 1e3 * cb["seconds"] / cb["steps"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": wl.config(1),
