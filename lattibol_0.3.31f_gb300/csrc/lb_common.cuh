@@ -187,20 +187,34 @@ __device__ __forceinline__ void d3q19_moments_native(const float (&g)[19], float
     uz = jz * inv;
 }
 
+// One opposite pair (g+, g-) of the native BGK for projection p, every step
+// a fused multiply-add: t = fma(4.5p, p, base), q+- = fma(+-3, p, t),
+// d+- = fma(a, q+-, -g+-) (f_eq - g in one rounding), g+- = fma(tau_inv, d+-,
+// g+-).  The two lanes run as paired FP32 FMAs (.f32x2, sm_100 and later),
+// each lane the scalar IEEE fma: the oracle's scalar fmaf gives the same bits.
+__device__ __forceinline__ void bgk_pair_native(float2 &gg, float a, float p, float base,
+                                                float tau_inv) {
+    const float t = __fmaf_rn(4.5f * p, p, base);
+    const float2 q = __ffma2_rn(make_float2(3.f, -3.f), make_float2(p, p), make_float2(t, t));
+    const float2 d = __ffma2_rn(make_float2(a, a), q, make_float2(-gg.x, -gg.y));
+    gg = __ffma2_rn(make_float2(tau_inv, tau_inv), d, gg);
+}
+
 // BGK at velocity (ux, uy, uz): per opposite pair with projection p,
 // t = 1 - 1.5 u^2 + 4.5 p^2 once, f_eq = w rho (t +- 3 p), f += tau_inv (f_eq - f)
+// (bgk_pair_native)
 __device__ __forceinline__ void d3q19_bgk_native(float (&g)[19], float ux, float uy, float uz,
                                                  float rho, float w0, float w1, float w7,
                                                  float tau_inv) {
     const float usq = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, ux * ux));
     const float base = __fmaf_rn(-1.5f, usq, 1.f);
     const float a0 = w0 * rho, a1 = w1 * rho, a7 = w7 * rho;
-    g[0] = __fmaf_rn(tau_inv, a0 * base - g[0], g[0]);
+    g[0] = __fmaf_rn(tau_inv, __fmaf_rn(a0, base, -g[0]), g[0]);
     auto pair = [&](int kp, int km, float a, float p) {
-        const float t = __fmaf_rn(4.5f * p, p, base);
-        const float fp = a * __fmaf_rn(3.f, p, t), fm = a * __fmaf_rn(-3.f, p, t);
-        g[kp] = __fmaf_rn(tau_inv, fp - g[kp], g[kp]);
-        g[km] = __fmaf_rn(tau_inv, fm - g[km], g[km]);
+        float2 gg = make_float2(g[kp], g[km]);
+        bgk_pair_native(gg, a, p, base, tau_inv);
+        g[kp] = gg.x;
+        g[km] = gg.y;
     };
     pair(1, 2, a1, ux);
     pair(3, 4, a1, uy);
@@ -310,12 +324,12 @@ __device__ __forceinline__ void d2q9_bgk_native(float (&g)[9], float ux, float u
     const float usq = __fmaf_rn(uy, uy, ux * ux);
     const float base = __fmaf_rn(-1.5f, usq, 1.f);
     const float a0 = w0 * rho, a1 = w1 * rho, a5 = w5 * rho;
-    g[0] = __fmaf_rn(tau_inv, a0 * base - g[0], g[0]);
+    g[0] = __fmaf_rn(tau_inv, __fmaf_rn(a0, base, -g[0]), g[0]);
     auto pair = [&](int kp, int km, float a, float p) {
-        const float t = __fmaf_rn(4.5f * p, p, base);
-        const float fp = a * __fmaf_rn(3.f, p, t), fm = a * __fmaf_rn(-3.f, p, t);
-        g[kp] = __fmaf_rn(tau_inv, fp - g[kp], g[kp]);
-        g[km] = __fmaf_rn(tau_inv, fm - g[km], g[km]);
+        float2 gg = make_float2(g[kp], g[km]);
+        bgk_pair_native(gg, a, p, base, tau_inv);
+        g[kp] = gg.x;
+        g[km] = gg.y;
     };
     pair(1, 3, a1, ux);
     pair(2, 4, a1, uy);

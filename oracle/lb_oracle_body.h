@@ -116,10 +116,12 @@ static inline void FN(d3q19_moments_native)(const R *g, R *rho, R *ux, R *uy, R 
 }
 static inline void FN(bgk_pair_native)(R *g, int kp, int km, R a, R p, R base, R tau_inv)
 {
+    /* every step a fused multiply-add; f_eq - g in one rounding */
     const R t = FMA_R((R)4.5f * p, p, base);
-    const R fp = a * FMA_R((R)3.f, p, t), fm = a * FMA_R((R)-3.f, p, t);
-    g[kp] = FMA_R(tau_inv, fp - g[kp], g[kp]);
-    g[km] = FMA_R(tau_inv, fm - g[km], g[km]);
+    const R dp = FMA_R(a, FMA_R((R)3.f, p, t), -g[kp]);
+    const R dm = FMA_R(a, FMA_R((R)-3.f, p, t), -g[km]);
+    g[kp] = FMA_R(tau_inv, dp, g[kp]);
+    g[km] = FMA_R(tau_inv, dm, g[km]);
 }
 static inline void FN(d3q19_bgk_native)(R *g, R ux, R uy, R uz, R rho, R w0, R w1, R w7,
                                         R tau_inv)
@@ -127,7 +129,7 @@ static inline void FN(d3q19_bgk_native)(R *g, R ux, R uy, R uz, R rho, R w0, R w
     const R usq = FMA_R(uz, uz, FMA_R(uy, uy, ux * ux));
     const R base = FMA_R((R)-1.5f, usq, (R)1.f);
     const R a0 = w0 * rho, a1 = w1 * rho, a7 = w7 * rho;
-    g[0] = FMA_R(tau_inv, a0 * base - g[0], g[0]);
+    g[0] = FMA_R(tau_inv, FMA_R(a0, base, -g[0]), g[0]);
     FN(bgk_pair_native)(g, 1, 2, a1, ux, base, tau_inv);
     FN(bgk_pair_native)(g, 3, 4, a1, uy, base, tau_inv);
     FN(bgk_pair_native)(g, 5, 6, a1, uz, base, tau_inv);
@@ -157,7 +159,7 @@ static inline void FN(d2q9_bgk_native)(R *g, R ux, R uy, R rho, R w0, R w1, R w5
     const R usq = FMA_R(uy, uy, ux * ux);
     const R base = FMA_R((R)-1.5f, usq, (R)1.f);
     const R a0 = w0 * rho, a1 = w1 * rho, a5 = w5 * rho;
-    g[0] = FMA_R(tau_inv, a0 * base - g[0], g[0]);
+    g[0] = FMA_R(tau_inv, FMA_R(a0, base, -g[0]), g[0]);
     FN(bgk_pair_native)(g, 1, 3, a1, ux, base, tau_inv);
     FN(bgk_pair_native)(g, 2, 4, a1, uy, base, tau_inv);
     FN(bgk_pair_native)(g, 5, 7, a5, ux + uy, base, tau_inv);
