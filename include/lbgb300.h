@@ -185,6 +185,11 @@ typedef enum {
 #define LB_TUNE_TBLOCK 0x020   /* D2Q9 native mode without Shan-Chen: temporal
                                   blocking, one launch advances several steps of a
                                   tile and its halo in shared memory */
+#define LB_TUNE_SC_STAGED 0x040 /* D3Q19 Shan-Chen on lattices without wall nodes
+                                   (nx a multiple of 32, ny of 8, nz of 4): the
+                                   single-pass step whose populations arrive in
+                                   shared memory by asynchronous copies issued
+                                   ahead of use; part of the default */
 #define LB_TUNE_TBLOCK_SHAPE(n) ((n) << 12) /* with LB_TUNE_TBLOCK: block shape 1..10
                                                (steps per launch x tile), 0 = the
                                                library's choice */

@@ -43,6 +43,7 @@ struct lb_ctx {
     bool closure_on = false;             // learned closure sets the local relaxation time
     ClosureArgs closure{};
     bool flags_set = false;
+    bool any_wall = false;               // some node carries CELL_WALL (flags start all fluid)
     int64_t launches = 0;
     int64_t steps = 0;                   // time steps since lb_create (or the checkpoint's)
     std::string err;
@@ -72,8 +73,10 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
 // Shan-Chen) measured 48.5 vs 24.1 GLUPS at 256^2, 11.1 vs 5.8 at 128^2 and
 // 73.3 vs 60.9 at 512^2, but 94.7 vs 101.5 at 1024^2 (a step then streams
 // from L2 faster than the blocks recompute their halos), so they are the
-// default up to TBLOCK_DEFAULT_MAX_NODES.
-constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE;
+// default up to TBLOCK_DEFAULT_MAX_NODES.  D3Q19 Shan-Chen without walls: the
+// staged single-pass step measured 28.6 / 34.1 / 34.2 GLUPS (FP32 / FP16 /
+// BF16) at 256^3 against 26.4 / 31.5 / 31.5 for the density pass + fused step.
+constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE | LB_TUNE_SC_STAGED;
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D2 = LB_TUNE_PDL;
 constexpr int TBLOCK_DEFAULT_SHAPE = 5;
 constexpr long TBLOCK_DEFAULT_MAX_NODES = 1L << 19;
@@ -122,6 +125,14 @@ cudaError_t mirror_sets(lb_ctx *c) {
 
 bool sc_on(const lb_ctx *c) {
     return c->cfg.mode == LB_MODE_REFERENCE ? (c->Q == 9 && c->cfg.G < 0.f) : c->cfg.G != 0.f;
+}
+
+// the D3Q19 Shan-Chen step runs as the single-pass kernel fed by bulk
+// asynchronous copies: native mode, no wall node, a lattice it tiles, and the
+// tuning asks for it
+bool sc_stage_on(const lb_ctx *c) {
+    return c->Q == 19 && c->cfg.mode == LB_MODE_NATIVE && sc_on(c) && !c->any_wall &&
+           (c->tune & LB_TUNE_SC_STAGED) && sc_stage_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz);
 }
 
 // the D2Q9 persistent step loop applies: no Shan-Chen pass and the tuning
@@ -233,6 +244,12 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
             return launch_d3q19_closure(a, ca, moments, c->stream);
         }
         const bool sc = sc_on(c);
+        if (sc_stage_on(c)) {
+            c->launches += 1;
+            a.err = c->psync;
+            c->persist_pending = true;  // a block that gave up waiting reports through psync[0]
+            return launch_d3q19_sc_stage(a, g.storage, moments, c->stream);
+        }
         if (sc && (c->tune & LB_TUNE_SC_SINGLE_PASS) && sc_march_chunk(g.nx, g.ny, g.nz)) {
             c->launches += 1;
             return launch_d3q19_sc_march(a, g.storage, moments, c->stream);
@@ -283,6 +300,7 @@ int graph_for(lb_ctx *c, int from, cudaGraphExec_t *out) {
 
 int launches_per_step(const lb_ctx *c) {
     if (!sc_on(c)) return 1;
+    if (sc_stage_on(c)) return 1;
     if (c->Q == 19 && c->cfg.mode == LB_MODE_NATIVE && (c->tune & LB_TUNE_SC_SINGLE_PASS) &&
         sc_march_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz))
         return 1;
@@ -454,6 +472,10 @@ int lb_set_flags(lb_ctx *c, const uint8_t *flags) {
     LB_TRY(c, "lb_set_flags", cudaMemcpyAsync(c->sb, sb.data(), c->N, cudaMemcpyHostToDevice, c->stream));
     LB_TRY(c, "lb_set_flags", cudaStreamSynchronize(c->stream));
     c->flags_set = true;
+    bool any_wall = false;
+    for (long o = 0; o < c->N && !any_wall; o++) any_wall = (f[o] & CELL_WALL) != 0;
+    if (any_wall != c->any_wall) drop_graphs(c);  // the step kernel may change
+    c->any_wall = any_wall;
     return LB_OK;
 }
 

@@ -30,6 +30,7 @@ struct D3Args {
     int psi_form;           // LB_PSI_REF or LB_PSI_EXP1
     float4 *probe;          // when set: (ux, uy, uz, rho) of node probe_o, every step
     int probe_o;            // (mapped host memory: the cursor read without a sync)
+    int *err;               // device error word of a kernel that waits on the GPU (or null)
 };
 
 struct D2Args {
@@ -58,6 +59,12 @@ cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc,
 // usable when sc_march_chunk(W, H, D) != 0
 int sc_march_chunk(int W, int H, int D);
 cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaStream_t s);
+// single-pass Shan-Chen step whose populations arrive by bulk asynchronous
+// copies (lb_sc_stage.cu); lattices without wall nodes for which
+// sc_stage_chunk(W, H, D) != 0.  A block that gives up waiting for its copies
+// sets *a.err (when a.err is set).
+int sc_stage_chunk(int W, int H, int D);
+cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom, cudaStream_t s);
 // equilibrium written in 16-bit deviation storage (storage 1 or 2; Pop holds
 // the storage arrays reinterpreted as float*)
 cudaError_t launch_d3q19_equilibrium_storage(const Pop<19> &p, const float *rho, const float *ux,

@@ -1,0 +1,304 @@
+// lb_sc_stage.cu -- single-pass D3Q19 Shan-Chen step for lattices without
+// wall nodes (the periodic spinodal case), fed by asynchronous copies into
+// shared memory.
+//
+// A block of 256 threads owns a 32 x 8 column tile and marches through a
+// chunk of z planes.  The populations reach shared memory as "stages": stage
+// z holds, for every population k, the 12 rows y0-2 .. y0+9 of plane z - c_z(k)
+// over the columns x0-A .. x0+31+A (A = one 16-byte unit of elements), i.e.
+// everything the pull of plane z reads for the tile and two rings around it.
+// The threads copy a stage in 16-byte cp.async chunks (each warp instruction
+// moves 512 contiguous bytes; periodic wrap is folded into each thread's chunk
+// addresses, formed once per block) and report on the slot's mbarrier when
+// their copies have landed.  Stages are issued two (FP32) or three (16-bit)
+// steps ahead of their use, so DRAM latency is covered by copies in flight
+// rather than by warps waiting on loads, and no global address is formed per
+// population and node.
+//
+// Step j of the march takes stage z = z0 - 1 + j: every thread pulls its own
+// node from it (kept in registers for the relaxation one step later) and the
+// first 84 threads also pull one node of the ring around the tile; each forms
+// psi(rho) into a four-plane psi buffer.  One barrier later the slot is
+// refilled with the stage SLOTS planes ahead and plane z - 1 is relaxed from
+// the kept populations and the psi stencil of planes z - 2 .. z.  Four psi
+// slots make that one barrier per plane enough (a warp writing psi of plane
+// z + 1 has passed the barrier of plane z, reached only after every warp
+// relaxed plane z - 2, the last reader of that slot).
+//
+// Arithmetic: the pulls read the same stored values as the two-pass step,
+// widened the same way; rho, the stencil sum and the relaxation are the same
+// device functions in the same order (d3q19_rho_native, d3q19_moments_native,
+// d3q19_sc_sum_native, d3q19_bgk_native), so the result is bit-identical to
+// the density pass + fused step.
+//
+// Every mbarrier wait is bounded; a block that gives up raises the device
+// error word, waits (bounded) for the copies it still has in flight and
+// returns.  (A first form copied each stage row with one cp.async.bulk per
+// population and row, 228 copies per stage: 20.9 GLUPS for FP32 and 16-bit
+// alike at 256^3, bound by the number of copies, not their bytes.)
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "lb_d3q19.cuh"
+#include "lb_tc05.cuh"
+
+namespace lb {
+
+namespace {
+
+constexpr int ST_TX = 32, ST_TY = 8;
+constexpr int ST_THREADS = ST_TX * ST_TY;             // 256
+constexpr int ST_RH = ST_TY + 4;                      // stage rows y0-2 .. y0+TY+1
+constexpr int ST_PX = ST_TX + 2, ST_PY = ST_TY + 2;   // psi region: tile + ring
+constexpr int ST_HALO = ST_PX * ST_PY - ST_THREADS;   // 84 ring nodes
+constexpr int ST_WAIT = 1 << 22;                      // mbarrier polls before giving up
+
+template <typename S>
+struct StageShape {
+    static constexpr int A = 16 / (int)sizeof(S);     // x margin: one 16-byte unit
+    static constexpr int RW = ST_TX + 2 * A;          // 40 (FP32) / 48 (16-bit) columns
+    static constexpr int POP = ST_RH * RW;            // elements of one population
+    static constexpr int ELEMS = 19 * POP;
+    static constexpr int BYTES = ELEMS * (int)sizeof(S);  // 36 480 / 21 888
+    static constexpr int SLOTS = sizeof(S) == 4 ? 2 : 3;
+    static constexpr int PSI_BYTES = 4 * ST_PY * ST_PX * (int)sizeof(float);
+    static constexpr int SMEM = SLOTS * BYTES + PSI_BYTES + SLOTS * 8;
+    static_assert(BYTES % 128 == 0 && PSI_BYTES % 16 == 0, "stage alignment");
+    static_assert((RW * (int)sizeof(S)) % 16 == 0, "bulk copies need 16-byte rows");
+};
+
+// the stored value of population k, widened as Store<S>::load does
+__device__ __forceinline__ float widen(float v, float) { return v; }
+__device__ __forceinline__ float widen(__half v, float wr) { return wr + __half2float(v); }
+__device__ __forceinline__ float widen(__nv_bfloat16 v, float wr) {
+    return wr + __bfloat162float(v);
+}
+
+// v in [-n, 2n): its periodic image in [0, n)
+__device__ __forceinline__ int wrap1(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// 16 bytes from global memory into shared memory (L2 only), asynchronously
+__device__ __forceinline__ void cp16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+// one arrival on mbar once every cp.async this thread issued so far has landed
+__device__ __forceinline__ void cp_arrive(uint64_t *mbar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+
+// populations with c_z = +1 / -1 as bit masks over k
+constexpr unsigned cz_mask(int sign) {
+    unsigned m = 0;
+    for (int k = 0; k < 19; k++) m |= (d3_cz(k) == sign ? 1u : 0u) << k;
+    return m;
+}
+constexpr unsigned kCzPos = cz_mask(1), kCzNeg = cz_mask(-1);
+static_assert(kCzPos == 0x2A220u && kCzNeg == 0x54440u, "D3Q19 z classes");
+
+// A stage is copied in 16-byte chunks: chunk c of a slot is bytes 16c .. 16c+15,
+// element (k, row, col) of the stage layout.  Thread t copies chunks t, t + 256,
+// ...; which global row and column each of its chunks reads does not change
+// from plane to plane, so the thread forms those addresses once (for plane 0,
+// with the chunk's z class -- plane z - c_z read for plane z -- in the two low
+// bits, free because every chunk address is 16-byte aligned).
+template <typename S>
+struct StageCopy {
+    using SS = StageShape<S>;
+    static constexpr int E = 16 / (int)sizeof(S);             // elements per chunk (= A)
+    static constexpr int CPR = SS::RW / E;                     // chunks per row: 10 / 6
+    static constexpr int CHUNKS = 19 * ST_RH * CPR;            // 2280 / 1368
+    static constexpr int PER_T = (CHUNKS + ST_THREADS - 1) / ST_THREADS;  // 9 / 6
+    const char *src[PER_T];
+
+    __device__ __forceinline__ StageCopy(const D3Args &a, int x0, int y0) {
+#pragma unroll
+        for (int i = 0; i < PER_T; i++) {
+            const int c = min((int)threadIdx.x + ST_THREADS * i, CHUNKS - 1);
+            const int R = c / CPR, q = c - R * CPR;
+            const int k = R / ST_RH, r = R - k * ST_RH;
+            const int cls = (kCzPos >> k & 1) ? 0 : ((kCzNeg >> k & 1) ? 2 : 1);  // c_z +1, 0, -1
+            const int yr = wrap1(y0 - 2 + r, a.H);
+            const int xm = wrap1(x0 - SS::A + q * E, a.W);
+            src[i] = reinterpret_cast<const char *>(a.src.f[k]) +
+                     ((long)yr * a.W + xm) * (long)sizeof(S) + cls;
+        }
+    }
+
+    // stage of plane zs into slot; one arrival per thread on mbar
+    __device__ __forceinline__ void issue(const D3Args &a, S *slot, uint64_t *mbar, int zs) const {
+        const long plane = (long)a.W * a.H * (long)sizeof(S);
+        // byte offset of the plane read by each z class, minus the class tag
+        const long o0 = wrap1(zs - 1, a.D) * plane, o1 = wrap1(zs, a.D) * plane - 1,
+                   o2 = wrap1(zs + 1, a.D) * plane - 2;
+        char *dst = reinterpret_cast<char *>(slot) + 16 * threadIdx.x;
+#pragma unroll
+        for (int i = 0; i < PER_T; i++) {
+            if (i == PER_T - 1 && (int)threadIdx.x + ST_THREADS * i >= CHUNKS) break;
+            const char *p = src[i];
+            const int cls = (int)(reinterpret_cast<uintptr_t>(p) & 3);
+            cp16(dst + 16 * ST_THREADS * i, p + (cls == 0 ? o0 : (cls == 1 ? o1 : o2)));
+        }
+        cp_arrive(mbar);
+    }
+};
+
+// the 19 post-stream populations of the node at stage column col, row row
+template <typename S>
+__device__ __forceinline__ void pull_stage(const S *st, int col, int row, const float *wr,
+                                           float (&g)[19]) {
+    using SS = StageShape<S>;
+#pragma unroll
+    for (int k = 0; k < 19; k++)
+        g[k] = widen(st[k * SS::POP + (row - d3_cy(k)) * SS::RW + col - d3_cx(k)], wr[k]);
+}
+
+__device__ __forceinline__ float psi_of(const D3Args &a, float rho) {
+    return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+}
+
+}  // namespace
+
+template <typename S, bool MOM>
+__global__ void __launch_bounds__(ST_THREADS, 2)
+    d3q19_sc_stage_kernel(const __grid_constant__ D3Args a, int zc) {
+    using SS = StageShape<S>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    S *stage = reinterpret_cast<S *>(smem);
+    float(*sp)[ST_PY][ST_PX] = reinterpret_cast<float(*)[ST_PY][ST_PX]>(smem + SS::SLOTS * SS::BYTES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + SS::SLOTS * SS::BYTES + SS::PSI_BYTES);
+
+    const int tid = threadIdx.x, tx = tid % ST_TX, ty = tid / ST_TX;
+    const int x0 = blockIdx.x * ST_TX, y0 = blockIdx.y * ST_TY, z0 = blockIdx.z * zc;
+    const int x = x0 + tx, y = y0 + ty;
+    // the ring node this thread also handles (tid < 84), relative to the tile:
+    // the two rows of 34, then the two side columns of 8
+    int hx = 0, hy = 0;
+    if (tid < 2 * ST_PX) {
+        hx = tid % ST_PX - 1;
+        hy = tid < ST_PX ? -1 : ST_TY;
+    } else if (tid < ST_HALO) {
+        hx = (tid - 2 * ST_PX) < ST_TY ? -1 : ST_TX;
+        hy = (tid - 2 * ST_PX) % ST_TY;
+    }
+
+    if (tid == 0)
+        for (int s = 0; s < SS::SLOTS; s++) mbar_init(&full[s], ST_THREADS);
+    __syncthreads();
+    const StageCopy<S> cp(a, x0, y0);
+    const int nst = zc + 2;  // stages z0 - 1 .. z0 + zc
+    for (int j = 0; j < SS::SLOTS && j < nst; j++)
+        cp.issue(a, stage + j * SS::ELEMS, &full[j], z0 - 1 + j);
+
+    float gs[19];  // own node, plane z - 1 (relaxed in this step)
+#pragma unroll
+    for (int k = 0; k < 19; k++) gs[k] = 0.f;
+    for (int j = 0; j < nst; j++) {
+        const int slot = j % SS::SLOTS;
+        const int zs = z0 - 1 + j;
+        const S *st = stage + slot * SS::ELEMS;
+        const bool ok = mbar_wait(&full[slot], (uint32_t)((j / SS::SLOTS) & 1), ST_WAIT);
+        float gn[19];
+#pragma unroll
+        for (int k = 0; k < 19; k++) gn[k] = 0.f;
+        float(*ps)[ST_PX] = sp[(zs + 4) & 3];
+        if (ok) {
+            pull_stage<S>(st, tx + SS::A, ty + 2, a.wr, gn);
+            ps[ty + 1][tx + 1] = psi_of(a, d3q19_rho_native(gn));
+            if (tid < ST_HALO) {
+                float gh[19];
+                pull_stage<S>(st, hx + SS::A, hy + 2, a.wr, gh);
+                ps[hy + 1][hx + 1] = psi_of(a, d3q19_rho_native(gh));
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            // give up: report, then wait (bounded) for the stages still in flight
+            if (tid == 0 && a.err) atomicExch(a.err, 1);
+            for (int i = j; i < j + SS::SLOTS && i < nst; i++)
+                mbar_wait(&full[i % SS::SLOTS], (uint32_t)((i / SS::SLOTS) & 1), ST_WAIT);
+            return;
+        }
+        if (j + SS::SLOTS < nst) cp.issue(a, stage + slot * SS::ELEMS, &full[slot], zs + SS::SLOTS);
+        if (j >= 2) {
+            const int z = zs - 1;
+            const int o = x + a.W * (y + a.H * z);
+            float rho, ux, uy, uz;
+            d3q19_moments_native(gs, rho, ux, uy, uz);
+            if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
+            const float inv_rt = 1.f / (rho * a.tau_inv);
+            float ex = ux, ey = uy, ez = uz;
+            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+            float pz[19];
+#pragma unroll
+            for (int k = 0; k < 19; k++)
+                pz[k] = sp[(z + d3_cz(k) + 4) & 3][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
+            float IFx, IFy, IFz;
+            d3q19_sc_sum_native(pz, a.w1, a.w7, IFx, IFy, IFz);
+            const float c = (-a.G * pz[0]) * inv_rt;
+            ex = __fmaf_rn(c, IFx, ex);
+            ey = __fmaf_rn(c, IFy, ey);
+            ez = __fmaf_rn(c, IFz, ez);
+            d3q19_bgk_native(gs, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+            S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
+#pragma unroll
+            for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, gs[k], a.wr[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 19; k++) gs[k] = gn[k];
+    }
+    // every wait has completed and no copy is in flight
+    if (tid == 0)
+        for (int s = 0; s < SS::SLOTS; s++) mbar_inval(&full[s]);
+}
+
+// z-chunk of the staged kernel, 0 if the lattice does not tile: the longest
+// march that still gives at least 1216 blocks (four waves of 2 blocks on 152
+// SMs), else the shortest that divides D
+int sc_stage_chunk(int W, int H, int D) {
+    if (W % ST_TX || H % ST_TY) return 0;
+    int pick = 0;
+    for (int zc : {32, 16, 8, 4}) {
+        if (D % zc) continue;
+        pick = zc;
+        if ((long)(W / ST_TX) * (H / ST_TY) * (D / zc) >= 1216) return zc;
+    }
+    return pick;
+}
+
+namespace {
+
+template <typename S>
+cudaError_t stage_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
+    using SS = StageShape<S>;
+    static_assert(SS::SMEM <= 113 * 1024, "two blocks per SM");
+    // once per instantiation
+    static const cudaError_t attr_e[2] = {
+        cudaFuncSetAttribute(d3q19_sc_stage_kernel<S, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM),
+        cudaFuncSetAttribute(d3q19_sc_stage_kernel<S, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM)};
+    if (attr_e[mom ? 1 : 0] != cudaSuccess) return attr_e[mom ? 1 : 0];
+    const dim3 g(a.W / ST_TX, a.H / ST_TY, a.D / zc);
+    if (mom) d3q19_sc_stage_kernel<S, true><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
+    else d3q19_sc_stage_kernel<S, false><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom, cudaStream_t s) {
+    const int zc = sc_stage_chunk(a.W, a.H, a.D);
+    if (!zc) return cudaErrorInvalidValue;
+    switch (storage) {
+    case 0: return stage_launch<float>(a, mom, zc, s);
+    case 1: return stage_launch<__half>(a, mom, zc, s);
+    case 2: return stage_launch<__nv_bfloat16>(a, mom, zc, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace lb
