@@ -61,6 +61,7 @@ struct StageShape {
     static constexpr int ELEMS = 19 * POP;
     static constexpr int BYTES = ELEMS * (int)sizeof(S);  // 36 480 / 21 888
     static constexpr int SLOTS = sizeof(S) == 4 ? 2 : 3;
+    static constexpr int MIN_BLOCKS = sizeof(S) == 4 ? 2 : 3;  // resident blocks per SM
     static constexpr int PSI_BYTES = 4 * ST_PY * ST_PX * (int)sizeof(float);
     static constexpr int SMEM = SLOTS * BYTES + PSI_BYTES + SLOTS * 8;
     static_assert(BYTES % 128 == 0 && PSI_BYTES % 16 == 0, "stage alignment");
@@ -161,7 +162,7 @@ __device__ __forceinline__ float psi_of(const D3Args &a, float rho) {
 }  // namespace
 
 template <typename S, bool MOM>
-__global__ void __launch_bounds__(ST_THREADS, 2)
+__global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
     d3q19_sc_stage_kernel(const __grid_constant__ D3Args a, int zc) {
     using SS = StageShape<S>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -191,17 +192,14 @@ __global__ void __launch_bounds__(ST_THREADS, 2)
     for (int j = 0; j < SS::SLOTS && j < nst; j++)
         cp.issue(a, stage + j * SS::ELEMS, &full[j], z0 - 1 + j);
 
-    float gs[19];  // own node, plane z - 1 (relaxed in this step)
-#pragma unroll
-    for (int k = 0; k < 19; k++) gs[k] = 0.f;
-    for (int j = 0; j < nst; j++) {
+    // step j: psi of plane z0 - 1 + j from its stage (the own node's populations
+    // into gn), then the relaxation of the plane before it from gs, pulled one
+    // step earlier; false when the block gave up waiting for its copies
+    auto step = [&](int j, float(&gs)[19], float(&gn)[19]) -> bool {
         const int slot = j % SS::SLOTS;
         const int zs = z0 - 1 + j;
         const S *st = stage + slot * SS::ELEMS;
         const bool ok = mbar_wait(&full[slot], (uint32_t)((j / SS::SLOTS) & 1), ST_WAIT);
-        float gn[19];
-#pragma unroll
-        for (int k = 0; k < 19; k++) gn[k] = 0.f;
         float(*ps)[ST_PX] = sp[(zs + 4) & 3];
         if (ok) {
             pull_stage<S>(st, tx + SS::A, ty + 2, a.wr, gn);
@@ -217,7 +215,7 @@ __global__ void __launch_bounds__(ST_THREADS, 2)
             if (tid == 0 && a.err) atomicExch(a.err, 1);
             for (int i = j; i < j + SS::SLOTS && i < nst; i++)
                 mbar_wait(&full[i % SS::SLOTS], (uint32_t)((i / SS::SLOTS) & 1), ST_WAIT);
-            return;
+            return false;
         }
         if (j + SS::SLOTS < nst) cp.issue(a, stage + slot * SS::ELEMS, &full[slot], zs + SS::SLOTS);
         if (j >= 2) {
@@ -247,9 +245,19 @@ __global__ void __launch_bounds__(ST_THREADS, 2)
 #pragma unroll
             for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, gs[k], a.wr[k]);
         }
+        return true;
+    };
+    // two steps per iteration with the population arrays swapped, so that no
+    // step copies the pulled populations from one array to the other
+    float ga[19], gb[19];
 #pragma unroll
-        for (int k = 0; k < 19; k++) gs[k] = gn[k];
+    for (int k = 0; k < 19; k++) ga[k] = gb[k] = 0.f;
+    int j = 0;
+    for (; j + 1 < nst; j += 2) {
+        if (!step(j, ga, gb)) return;
+        if (!step(j + 1, gb, ga)) return;
     }
+    if (j < nst && !step(j, ga, gb)) return;
     // every wait has completed and no copy is in flight
     if (tid == 0)
         for (int s = 0; s < SS::SLOTS; s++) mbar_inval(&full[s]);
@@ -274,7 +282,7 @@ namespace {
 template <typename S>
 cudaError_t stage_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
     using SS = StageShape<S>;
-    static_assert(SS::SMEM <= 113 * 1024, "two blocks per SM");
+    static_assert(SS::MIN_BLOCKS * (SS::SMEM + 1024) <= 228 * 1024, "resident blocks per SM");
     // once per instantiation
     static const cudaError_t attr_e[2] = {
         cudaFuncSetAttribute(d3q19_sc_stage_kernel<S, false>,
