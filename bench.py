@@ -177,9 +177,11 @@ def run_ensemble(args, dist, ws, rank, local):
                        % ENSEMBLE["seed"], "G": "U[-5.5,-4.5]", "tau": 1.0,
                        "psi": "1-exp(-rho)",
                        "launch_shape": ({("single_pass_tiles" if shape[1] <= 5 else
-                                          "single_pass_warp_strips"):
+                                          "single_pass_warp_strips" if shape[1] <= 9 else
+                                          "single_pass_warp_strips_smem_row_ring"):
                                          "32x%d" % {1: 8, 2: 8, 3: 16, 4: 16, 5: 32, 6: 32,
-                                                    7: 32, 8: 64, 9: 16}[shape[1]],
+                                                    7: 32, 8: 64, 9: 16, 10: 32, 11: 64,
+                                                    12: 16}[shape[1]],
                                          "shape": shape[1], "blocks_per_sm": shape[2]}
                                         if shape[0] == 0 else
                                         {"threads_x": shape[0], "rows_per_item": shape[1],

@@ -226,45 +226,195 @@ __device__ __forceinline__ float ens_psi(const EnsArgs &a, float rho) {
     return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
+// one strip item (march of R rows of 32 columns) by one warp, plain loads
+template <int R, bool MOM>
+__device__ __forceinline__ void ens_march_item(const EnsArgs &a, const EnsItem dm, int lane) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const bool edge = lane == 0 || lane == 31;
+    const bool small = dm.W < ET_PX;
+    const int x = ens_wrap(dm.x + lane, dm.W, small);
+    const int xh = ens_wrap(lane == 0 ? dm.x - 1 : dm.x + ET_BX, dm.W, small);
+    const bool own = dm.x + lane < dm.W;
+    const int y_end = min(dm.y + R, dm.H);
+    float gc[9], rc, uxc, uyc;  // row r: pulled populations and moments at x
+    float pm, pc, hm = 0.f, hc = 0.f;  // psi of rows r - 1, r (h: the halo column)
+    {
+        float g[9];
+        const int ym = ens_wrap(dm.y - 1, dm.H, false);
+        ens_pull(a, dm, x, ym, g);
+        pm = ens_psi(a, d2q9_rho_native(g));
+        ens_pull(a, dm, x, dm.y, gc);
+        d2q9_moments_native(gc, rc, uxc, uyc);
+        pc = ens_psi(a, rc);
+        if (edge) {
+            ens_pull(a, dm, xh, ym, g);
+            hm = ens_psi(a, d2q9_rho_native(g));
+            ens_pull(a, dm, xh, dm.y, g);
+            hc = ens_psi(a, d2q9_rho_native(g));
+        }
+    }
+    for (int r = dm.y; r < y_end; r++) {
+        const int yp = ens_wrap(r + 1, dm.H, false);
+        float gn[9], rn, uxn, uyn, hn = 0.f;
+        ens_pull(a, dm, x, yp, gn);
+        if (edge) {
+            float g[9];
+            ens_pull(a, dm, xh, yp, g);
+            hn = ens_psi(a, d2q9_rho_native(g));
+        }
+        d2q9_moments_native(gn, rn, uxn, uyn);
+        const float pn = ens_psi(a, rn);
+        // x - 1 and x + 1 from the neighbour lanes, the halo at the strip ends
+        float lm = __shfl_up_sync(FULL, pm, 1), lc = __shfl_up_sync(FULL, pc, 1);
+        float ln = __shfl_up_sync(FULL, pn, 1);
+        float qm = __shfl_down_sync(FULL, pm, 1), qc = __shfl_down_sync(FULL, pc, 1);
+        float qn = __shfl_down_sync(FULL, pn, 1);
+        if (lane == 0) { lm = hm; lc = hc; ln = hn; }
+        if (lane == 31) { qm = hm; qc = hc; qn = hn; }
+        if (own) {
+            // the fused pass's order: psi(x), psi(x+1,y), psi(x,row+1),
+            // psi(x-1,y), psi(x,row-1), then the diagonals
+            const float ps[9] = {pc, qc, pn, lc, pm, qn, ln, lm, qm};
+            float ex = uxc, ey = uyc;
+            d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rc), ex, ey);
+            d2q9_bgk_native(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
+            const int o = dm.off + x + dm.W * r;
+            if (MOM) { a.rho[o] = rc; a.ux[o] = uxc; a.uy[o] = uyc; }
+#pragma unroll
+            for (int k = 0; k < 9; k++) a.dst[k][o] = gc[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) gc[k] = gn[k];
+        rc = rn; uxc = uxn; uyc = uyn;
+        pm = pc; pc = pn; hm = hc; hc = hn;
+    }
+}
+
 template <int R, int MINB, bool MOM>
 __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(const EnsArgs a) {
-    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int warps_per_block = ENS_MARCH_THREADS / 32;
     const int nwarps = gridDim.x * warps_per_block;
-    const bool edge = lane == 0 || lane == 31;
     for (int it = blockIdx.x * warps_per_block + (threadIdx.x >> 5); it < a.nitems;
-         it += nwarps) {
+         it += nwarps)
+        ens_march_item<R, MOM>(a, a.items[it], lane);
+}
+
+// ---------------------------------------------------------------------------
+// Strips with a shared-memory row ring.  The march above must wait for the
+// loads of row r + 1 before it can relax row r: a DRAM latency per row for
+// every warp.  Here each warp keeps the source rows its pulls read in a ring
+// of ENS_RING slots in shared memory (9 populations x 40 columns: the strip,
+// the two halo columns and their outer neighbours, rounded out to 16-byte
+// chunks) and copies source row r + 4 with 16-byte cp.async (one commit group
+// per row) before it pulls row r + 1, so rows land two rows ahead of their
+// use and the pulls are shared-memory loads.  A lane waits for its own groups
+// (cp.async.wait_group) and a warp barrier makes every lane's copies visible;
+// no block barrier.  An item qualifies when its domain's rows start on 16
+// bytes and no chunk straddles its periodic x edge (W a multiple of 32, first
+// node a multiple of 4); other items take the plain march.  Same pulls and
+// arithmetic as the march, so the same bits.
+// ---------------------------------------------------------------------------
+constexpr int ENS_RING = 6;                    // source-row slots per warp
+constexpr int ENS_RCOLS = ET_BX + 8;           // columns x0 - 4 .. x0 + 35
+constexpr int ENS_RROW = 9 * ENS_RCOLS;        // floats per slot (90 chunks of 16 bytes)
+constexpr int ENS_RING_SMEM = ENS_RING * ENS_RROW * 4 * (ENS_MARCH_THREADS / 32);  // 69 120 B
+
+__device__ __forceinline__ void ens_cp16(float *dst, const float *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void ens_cp_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// this lane's commit groups except the newest N have landed
+template <int N>
+__device__ __forceinline__ void ens_cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int R, int MINB, bool MOM>
+__global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_ring_kernel(const EnsArgs a) {
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ __align__(16) float ens_ring_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *const ring = ens_ring_smem + warp * ENS_RING * ENS_RROW;
+    const int warps_per_block = ENS_MARCH_THREADS / 32;
+    const int nwarps = gridDim.x * warps_per_block;
+    const bool edge = lane == 0 || lane == 31;
+    const int col = 4 + lane, hcol = lane == 0 ? 3 : 4 + ET_BX;  // ring columns of x, xh
+    for (int it = blockIdx.x * warps_per_block + warp; it < a.nitems; it += nwarps) {
         const EnsItem dm = a.items[it];
-        const bool small = dm.W < ET_PX;
-        const int x = ens_wrap(dm.x + lane, dm.W, small);
-        const int xh = ens_wrap(lane == 0 ? dm.x - 1 : dm.x + ET_BX, dm.W, small);
-        const bool own = dm.x + lane < dm.W;
+        if ((dm.W & 31) || (dm.off & 3)) {
+            ens_march_item<R, MOM>(a, dm, lane);
+            continue;
+        }
         const int y_end = min(dm.y + R, dm.H);
+        const bool small_h = dm.H < 4;
+        // this lane's chunks of a source row (chunk c = 10 k + q: population k,
+        // columns x0 - 4 + 4q .. + 3), addresses in row 0 of the domain
+        const float *cs[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const int c = min(lane + 32 * i, 89);
+            const int k = c / 10, q = c - 10 * k;
+            cs[i] = a.src[k] + dm.off + ens_wrap(dm.x - 4 + 4 * q, dm.W, false);
+        }
+        const int base = dm.y - 2;  // source row sr lives in slot (sr - base) % ENS_RING
+        auto slot = [&](int sr) { return ring + ((sr - base) % ENS_RING) * ENS_RROW; };
+        // source row sr into its slot as one commit group (empty past the item)
+        auto issue = [&](int sr) {
+            if (sr <= y_end + 1) {
+                const long row = (long)dm.W * ens_wrap(sr, dm.H, small_h);
+                float *sl = slot(sr);
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+                    if (lane + 32 * i < 90) ens_cp16(sl + 4 * (lane + 32 * i), cs[i] + row);
+            }
+            ens_cp_commit();
+        };
+        // pull of ring column cl for row p: population k from row p - cr_k, column cl - cx_k
+        auto pull = [&](int cl, int p, float(&g)[9]) {
+            const float *sm = slot(p - 1), *s0 = slot(p), *sp = slot(p + 1);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const float *sl = d2_cr(k) > 0 ? sm : (d2_cr(k) < 0 ? sp : s0);
+                g[k] = sl[k * ENS_RCOLS + cl - d2_cx(k)];
+            }
+        };
+#pragma unroll
+        for (int i = 0; i < ENS_RING; i++) issue(base + i);  // source rows y - 2 .. y + 3
+        ens_cp_wait<2>();  // rows y - 2 .. y + 1 have landed
+        __syncwarp();
         float gc[9], rc, uxc, uyc;  // row r: pulled populations and moments at x
         float pm, pc, hm = 0.f, hc = 0.f;  // psi of rows r - 1, r (h: the halo column)
         {
             float g[9];
-            const int ym = ens_wrap(dm.y - 1, dm.H, false);
-            ens_pull(a, dm, x, ym, g);
+            pull(col, dm.y - 1, g);
             pm = ens_psi(a, d2q9_rho_native(g));
-            ens_pull(a, dm, x, dm.y, gc);
+            pull(col, dm.y, gc);
             d2q9_moments_native(gc, rc, uxc, uyc);
             pc = ens_psi(a, rc);
             if (edge) {
-                ens_pull(a, dm, xh, ym, g);
+                pull(hcol, dm.y - 1, g);
                 hm = ens_psi(a, d2q9_rho_native(g));
-                ens_pull(a, dm, xh, dm.y, g);
+                pull(hcol, dm.y, g);
                 hc = ens_psi(a, d2q9_rho_native(g));
             }
         }
+        const int x = dm.x + lane;
         for (int r = dm.y; r < y_end; r++) {
-            const int yp = ens_wrap(r + 1, dm.H, false);
+            __syncwarp();  // every lane is done with the slot of source row r - 2
+            issue(r + 4);
+            ens_cp_wait<2>();  // source row r + 2 has landed
+            __syncwarp();
             float gn[9], rn, uxn, uyn, hn = 0.f;
-            ens_pull(a, dm, x, yp, gn);
+            pull(col, r + 1, gn);
             if (edge) {
                 float g[9];
-                ens_pull(a, dm, xh, yp, g);
+                pull(hcol, r + 1, g);
                 hn = ens_psi(a, d2q9_rho_native(g));
             }
             d2q9_moments_native(gn, rn, uxn, uyn);
@@ -276,24 +426,51 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(cons
             float qn = __shfl_down_sync(FULL, pn, 1);
             if (lane == 0) { lm = hm; lc = hc; ln = hn; }
             if (lane == 31) { qm = hm; qc = hc; qn = hn; }
-            if (own) {
-                // the fused pass's order: psi(x), psi(x+1,y), psi(x,row+1),
-                // psi(x-1,y), psi(x,row-1), then the diagonals
-                const float ps[9] = {pc, qc, pn, lc, pm, qn, ln, lm, qm};
-                float ex = uxc, ey = uyc;
-                d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rc), ex, ey);
-                d2q9_bgk_native(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
-                const int o = dm.off + x + dm.W * r;
-                if (MOM) { a.rho[o] = rc; a.ux[o] = uxc; a.uy[o] = uyc; }
+            const float ps[9] = {pc, qc, pn, lc, pm, qn, ln, lm, qm};
+            float ex = uxc, ey = uyc;
+            d2q9_sc_shift_native(ps, a.w1, a.w5, dm.G, 1.f / (dm.tau_inv * rc), ex, ey);
+            d2q9_bgk_native(gc, ex, ey, rc, a.w0, a.w1, a.w5, dm.tau_inv);
+            const int o = dm.off + x + dm.W * r;
+            if (MOM) { a.rho[o] = rc; a.ux[o] = uxc; a.uy[o] = uyc; }
 #pragma unroll
-                for (int k = 0; k < 9; k++) a.dst[k][o] = gc[k];
-            }
+            for (int k = 0; k < 9; k++) a.dst[k][o] = gc[k];
 #pragma unroll
             for (int k = 0; k < 9; k++) gc[k] = gn[k];
             rc = rn; uxc = uxn; uyc = uyn;
             pm = pc; pc = pn; hm = hc; hc = hn;
         }
+        __syncwarp();  // the next item's copies overwrite slots this item read
     }
+}
+
+// ring strip shapes: rows per item and the register bound (resident blocks per SM)
+#define LB_ENS_RING(X) \
+    X(10, 32, 3)       \
+    X(11, 64, 3)       \
+    X(12, 16, 3)
+
+int ens_ring_rows(int shape) {
+    switch (shape) {
+#define LB_ENS_RROWS(S, R, MINB) \
+    case S: return R;
+        LB_ENS_RING(LB_ENS_RROWS)
+#undef LB_ENS_RROWS
+        default: return 0;
+    }
+}
+
+template <int R, int MINB>
+cudaError_t ens_ring_launch(const EnsArgs &a, bool mom, unsigned grid, cudaStream_t s) {
+    // once per instantiation
+    static const cudaError_t attr_e[2] = {
+        cudaFuncSetAttribute(ens_ring_kernel<R, MINB, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, ENS_RING_SMEM),
+        cudaFuncSetAttribute(ens_ring_kernel<R, MINB, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, ENS_RING_SMEM)};
+    if (attr_e[mom ? 1 : 0] != cudaSuccess) return attr_e[mom ? 1 : 0];
+    if (mom) ens_ring_kernel<R, MINB, true><<<grid, ENS_MARCH_THREADS, ENS_RING_SMEM, s>>>(a);
+    else ens_ring_kernel<R, MINB, false><<<grid, ENS_MARCH_THREADS, ENS_RING_SMEM, s>>>(a);
+    return cudaGetLastError();
 }
 
 // march shapes: rows per item and the register bound (resident blocks per SM)
@@ -347,7 +524,10 @@ struct lb_ensemble {
     EnsItem *items_d = nullptr;
     int nitems = 0, items_cap = 0;
     int cur = 0, psi_form = LB_PSI_EXP1, sms = 1, graph_steps = 32;
-    LaunchShape shape{0, 6, 3};  // single-pass warp strips of 32 rows, 3 blocks per SM
+    // single-pass warp strips of 32 rows with the shared-memory row ring, 3
+    // blocks per SM: 72.4 GLUPS on 512 droplet domains, against 63.2 for the
+    // strips with plain loads (shape 6)
+    LaunchShape shape{0, 10, 3};
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -408,6 +588,14 @@ cudaError_t ens_step(lb_ensemble *e, int from, bool mom) {
         break;
             LB_ENS_MARCH(LB_ENS_MLAUNCH)
 #undef LB_ENS_MLAUNCH
+#define LB_ENS_RLAUNCH(S, R, MINB)                                                             \
+    case S: {                                                                                  \
+        const cudaError_t c = ens_ring_launch<R, MINB>(a, mom, grid, e->stream);               \
+        if (c != cudaSuccess) return c;                                                        \
+        break;                                                                                 \
+    }
+            LB_ENS_RING(LB_ENS_RLAUNCH)
+#undef LB_ENS_RLAUNCH
             default: return cudaErrorInvalidValue;
         }
         e->launches += 1;
@@ -437,7 +625,8 @@ int build_items(lb_ensemble *e) {
     for (int d = 0; d < e->nd; d++) {
         const EnsDomain &m = e->dom[d];
         if (e->shape.bx == 0) {  // tiles or strips, row by row
-            const int rows = ens_tile_rows(e->shape.ry) + ens_march_rows(e->shape.ry);
+            const int rows = ens_tile_rows(e->shape.ry) + ens_march_rows(e->shape.ry) +
+                             ens_ring_rows(e->shape.ry);
             for (int y = 0; y < m.H; y += rows)
                 for (int x = 0; x < m.W; x += ET_BX)
                     items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, x});
@@ -629,7 +818,7 @@ int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy) {
 int lb_ensemble_set_launch(lb_ensemble *e, int threads_x, int rows, int blocks_per_sm) {
     const bool tiles = threads_x == 0;
     if (!e || blocks_per_sm < 1 || blocks_per_sm > 32 ||
-        (tiles && ens_tile_rows(rows) + ens_march_rows(rows) == 0) ||
+        (tiles && ens_tile_rows(rows) + ens_march_rows(rows) + ens_ring_rows(rows) == 0) ||
         (!tiles && (threads_x < 32 || threads_x % 32 || rows < 1 || threads_x * rows > 1024)))
         return LB_ERR_ARG;
     LB_ETRY(e, "lb_ensemble_set_launch", cudaStreamSynchronize(e->stream));
@@ -655,7 +844,8 @@ int lb_ensemble_autotune(lb_ensemble *e, int trial_steps, int out[3]) {
     // (tile or strip shape, blocks per SM): each shape at its register-bound
     // residency and at twice it
     static const int TILES[][2] = {{1, 5}, {1, 10}, {2, 6}, {2, 12}, {3, 2}, {3, 4}, {4, 3},
-                                   {5, 1}, {6, 3}, {6, 6}, {7, 4}, {7, 8}, {8, 3}, {9, 3}};
+                                   {5, 1}, {6, 3}, {6, 6}, {7, 4}, {7, 8}, {8, 3}, {9, 3},
+                                   {10, 3}, {11, 3}, {12, 3}};
     std::vector<LaunchShape> cand;
     for (const auto &t : TILES) cand.push_back(LaunchShape{0, t[0], t[1]});
     for (int i = 0; i < 3; i++)
