@@ -362,22 +362,24 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_ring_kernel(const
             const int k = c / 10, q = c - 10 * k;
             cs[i] = a.src[k] + dm.off + ens_wrap(dm.x - 4 + 4 * q, dm.W, false);
         }
-        const int base = dm.y - 2;  // source row sr lives in slot (sr - base) % ENS_RING
-        auto slot = [&](int sr) { return ring + ((sr - base) % ENS_RING) * ENS_RROW; };
-        // source row sr into its slot as one commit group (empty past the item)
-        auto issue = [&](int sr) {
+        // source row sr of the item lives in slot (sr - (y - 2)) % ENS_RING
+        auto slot = [&](int i) { return ring + i * ENS_RROW; };
+        // source row sr into slot i as one commit group (empty past the item)
+        auto issue = [&](int sr, int i) {
             if (sr <= y_end + 1) {
                 const long row = (long)dm.W * ens_wrap(sr, dm.H, small_h);
-                float *sl = slot(sr);
+                float *sl = slot(i);
 #pragma unroll
-                for (int i = 0; i < 3; i++)
-                    if (lane + 32 * i < 90) ens_cp16(sl + 4 * (lane + 32 * i), cs[i] + row);
+                for (int j = 0; j < 3; j++)
+                    if (lane + 32 * j < 90) ens_cp16(sl + 4 * (lane + 32 * j), cs[j] + row);
             }
             ens_cp_commit();
         };
-        // pull of ring column cl for row p: population k from row p - cr_k, column cl - cx_k
-        auto pull = [&](int cl, int p, float(&g)[9]) {
-            const float *sm = slot(p - 1), *s0 = slot(p), *sp = slot(p + 1);
+        // pull of ring column cl of the row whose upstream rows (row - 1, row,
+        // row + 1) sit in slots im, i0, ip: population k from row - cr_k,
+        // column cl - cx_k
+        auto pull = [&](int cl, int im, int i0, int ip, float(&g)[9]) {
+            const float *sm = slot(im), *s0 = slot(i0), *sp = slot(ip);
 #pragma unroll
             for (int k = 0; k < 9; k++) {
                 const float *sl = d2_cr(k) > 0 ? sm : (d2_cr(k) < 0 ? sp : s0);
@@ -385,38 +387,42 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_ring_kernel(const
             }
         };
 #pragma unroll
-        for (int i = 0; i < ENS_RING; i++) issue(base + i);  // source rows y - 2 .. y + 3
-        ens_cp_wait<2>();  // rows y - 2 .. y + 1 have landed
+        for (int i = 0; i < ENS_RING; i++) issue(dm.y - 2 + i, i);  // source rows y - 2 .. y + 3
+        ens_cp_wait<ENS_RING - 4>();  // rows y - 2 .. y + 1 have landed
         __syncwarp();
         float gc[9], rc, uxc, uyc;  // row r: pulled populations and moments at x
         float pm, pc, hm = 0.f, hc = 0.f;  // psi of rows r - 1, r (h: the halo column)
         {
             float g[9];
-            pull(col, dm.y - 1, g);
+            pull(col, 0, 1, 2, g);
             pm = ens_psi(a, d2q9_rho_native(g));
-            pull(col, dm.y, gc);
+            pull(col, 1, 2, 3, gc);
             d2q9_moments_native(gc, rc, uxc, uyc);
             pc = ens_psi(a, rc);
             if (edge) {
-                pull(hcol, dm.y - 1, g);
+                pull(hcol, 0, 1, 2, g);
                 hm = ens_psi(a, d2q9_rho_native(g));
-                pull(hcol, dm.y, g);
+                pull(hcol, 1, 2, 3, g);
                 hc = ens_psi(a, d2q9_rho_native(g));
             }
         }
+        auto next = [](int i) { return i == ENS_RING - 1 ? 0 : i + 1; };
+        int i0 = 2;  // slot of source row r
         const int x = dm.x + lane;
         for (int r = dm.y; r < y_end; r++) {
+            const int i1 = next(i0), i2 = next(i1);
             __syncwarp();  // every lane is done with the slot of source row r - 2
-            issue(r + 4);
-            ens_cp_wait<2>();  // source row r + 2 has landed
+            issue(r + ENS_RING - 2, i0 >= 2 ? i0 - 2 : i0 + ENS_RING - 2);
+            ens_cp_wait<ENS_RING - 4>();  // source row r + 2 has landed
             __syncwarp();
             float gn[9], rn, uxn, uyn, hn = 0.f;
-            pull(col, r + 1, gn);
+            pull(col, i0, i1, i2, gn);
             if (edge) {
                 float g[9];
-                pull(hcol, r + 1, g);
+                pull(hcol, i0, i1, i2, g);
                 hn = ens_psi(a, d2q9_rho_native(g));
             }
+            i0 = i1;
             d2q9_moments_native(gn, rn, uxn, uyn);
             const float pn = ens_psi(a, rn);
             // x - 1 and x + 1 from the neighbour lanes, the halo at the strip ends
