@@ -282,9 +282,12 @@ int lb_ensemble_get_moments(lb_ensemble *e, float *rho, float *ux, float *uy);
  * form: 1..5 tiles that form psi of the tile and its ring in shared memory
  * (1: 32 x 8 at 48 registers; 2: 32 x 8 at 40; 3: 32 x 16 at 60; 4: 32 x 16
  * at 40; 5: 32 x 32 at 60), 6..9 warps marching down 32-column strips with
- * psi of three rows in registers (6: 32 rows at 80 registers, the default
- * with 3 blocks per SM; 7: 32 rows at 64; 8: 64 rows; 9: 16 rows).
- * Otherwise the two-pass step (psi pass, fused pass)
+ * psi of three rows in registers (6: 32 rows at 80 registers; 7: 32 rows at
+ * 64; 8: 64 rows; 9: 16 rows), 10..12 the same strips fed by a per-warp
+ * shared-memory ring of source rows copied ahead with cp.async (10: 32 rows,
+ * the default with 3 blocks per SM; 11: 64 rows; 12: 16 rows; domains not a
+ * multiple of 32 wide, or not starting on a 16-byte boundary, take the plain
+ * strips).  Otherwise the two-pass step (psi pass, fused pass)
  * over groups of `rows` rows with threads_x threads along x (a multiple of
  * 32).  Both give the same bits.  The autotuner times every candidate for
  * trial_steps steps on the ensemble itself (advancing its state: tune before
