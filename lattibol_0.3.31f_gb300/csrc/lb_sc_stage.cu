@@ -48,24 +48,36 @@ namespace {
 
 constexpr int ST_TX = 32, ST_TY = 8;
 constexpr int ST_THREADS = ST_TX * ST_TY;             // 256
-constexpr int ST_RH = ST_TY + 4;                      // stage rows y0-2 .. y0+TY+1
 constexpr int ST_PX = ST_TX + 2, ST_PY = ST_TY + 2;   // psi region: tile + ring
 constexpr int ST_HALO = ST_PX * ST_PY - ST_THREADS;   // 84 ring nodes
 constexpr int ST_WAIT = 1 << 22;                      // mbarrier polls before giving up
 
+// Stage layout.  Population k of a stage holds the 10 rows its pulls read for
+// the tile and its ring (rows y0-1-c_y .. y0+8-c_y of plane z - c_z) over the
+// columns they read (x0-1-c_x .. x0+32-c_x) rounded out to whole 16-byte
+// chunks: 32 + 2E columns for c_x = 0, 32 + E otherwise (E elements per
+// chunk).  The populations follow one another, row by row.
 template <typename S>
 struct StageShape {
-    static constexpr int A = 16 / (int)sizeof(S);     // x margin: one 16-byte unit
-    static constexpr int RW = ST_TX + 2 * A;          // 40 (FP32) / 48 (16-bit) columns
-    static constexpr int POP = ST_RH * RW;            // elements of one population
-    static constexpr int ELEMS = 19 * POP;
-    static constexpr int BYTES = ELEMS * (int)sizeof(S);  // 36 480 / 21 888
+    static constexpr int E = 16 / (int)sizeof(S);      // elements per 16-byte chunk
+    static constexpr int ROWS = ST_TY + 2;             // rows of every population
+    // first column relative to x0, and width, of population k
+    static constexpr int col0(int k) { return d3_cx(k) < 0 ? 0 : -E; }
+    static constexpr int width(int k) { return d3_cx(k) == 0 ? ST_TX + 2 * E : ST_TX + E; }
+    static constexpr int chunks(int k) { return ROWS * width(k) / E; }
+    static constexpr int first_chunk(int k) {
+        int c = 0;
+        for (int j = 0; j < k; j++) c += chunks(j);
+        return c;
+    }
+    static constexpr int CHUNKS = first_chunk(19);       // 1800 (FP32) / 1040 (16-bit)
+    static constexpr int ELEMS = CHUNKS * E;
+    static constexpr int BYTES = CHUNKS * 16;            // 28 800 / 16 640
     static constexpr int SLOTS = sizeof(S) == 4 ? 2 : 3;
-    static constexpr int MIN_BLOCKS = sizeof(S) == 4 ? 2 : 3;  // resident blocks per SM
+    static constexpr int MIN_BLOCKS = 3;                  // resident blocks per SM
     static constexpr int PSI_BYTES = 4 * ST_PY * ST_PX * (int)sizeof(float);
     static constexpr int SMEM = SLOTS * BYTES + PSI_BYTES + SLOTS * 8;
     static_assert(BYTES % 128 == 0 && PSI_BYTES % 16 == 0, "stage alignment");
-    static_assert((RW * (int)sizeof(S)) % 16 == 0, "bulk copies need 16-byte rows");
 };
 
 // the stored value of population k, widened as Store<S>::load does
@@ -89,7 +101,7 @@ __device__ __forceinline__ void cp_arrive(uint64_t *mbar) {
                  : "memory");
 }
 
-// populations with c_z = +1 / -1 as bit masks over k
+// populations with c_z (c_y) = +1 / -1 as bit masks over k
 constexpr unsigned cz_mask(int sign) {
     unsigned m = 0;
     for (int k = 0; k < 19; k++) m |= (d3_cz(k) == sign ? 1u : 0u) << k;
@@ -97,6 +109,12 @@ constexpr unsigned cz_mask(int sign) {
 }
 constexpr unsigned kCzPos = cz_mask(1), kCzNeg = cz_mask(-1);
 static_assert(kCzPos == 0x2A220u && kCzNeg == 0x54440u, "D3Q19 z classes");
+constexpr unsigned cy_mask(int sign) {
+    unsigned m = 0;
+    for (int k = 0; k < 19; k++) m |= (d3_cy(k) == sign ? 1u : 0u) << k;
+    return m;
+}
+constexpr unsigned kCyPos = cy_mask(1), kCyNeg = cy_mask(-1);
 
 // A stage is copied in 16-byte chunks: chunk c of a slot is bytes 16c .. 16c+15,
 // element (k, row, col) of the stage layout.  Thread t copies chunks t, t + 256,
@@ -107,21 +125,30 @@ static_assert(kCzPos == 0x2A220u && kCzNeg == 0x54440u, "D3Q19 z classes");
 template <typename S>
 struct StageCopy {
     using SS = StageShape<S>;
-    static constexpr int E = 16 / (int)sizeof(S);             // elements per chunk (= A)
-    static constexpr int CPR = SS::RW / E;                     // chunks per row: 10 / 6
-    static constexpr int CHUNKS = 19 * ST_RH * CPR;            // 2280 / 1368
-    static constexpr int PER_T = (CHUNKS + ST_THREADS - 1) / ST_THREADS;  // 9 / 6
+    static constexpr int E = SS::E;
+    static constexpr int CHUNKS = SS::CHUNKS;
+    static constexpr int PER_T = (CHUNKS + ST_THREADS - 1) / ST_THREADS;  // 8 / 5
     const char *src[PER_T];
 
     __device__ __forceinline__ StageCopy(const D3Args &a, int x0, int y0) {
 #pragma unroll
         for (int i = 0; i < PER_T; i++) {
             const int c = min((int)threadIdx.x + ST_THREADS * i, CHUNKS - 1);
-            const int R = c / CPR, q = c - R * CPR;
-            const int k = R / ST_RH, r = R - k * ST_RH;
+            // population k of chunk c, its first chunk, chunks per row, first column
+            int k = 0, c0 = 0, cpr = SS::width(0) / E, x_0 = SS::col0(0);
+#pragma unroll
+            for (int j = 1; j < 19; j++)
+                if (c >= SS::first_chunk(j)) {
+                    k = j;
+                    c0 = SS::first_chunk(j);
+                    cpr = SS::width(j) / E;
+                    x_0 = SS::col0(j);
+                }
+            const int r = (c - c0) / cpr, q = c - c0 - r * cpr;
+            const int cy = (kCyPos >> k & 1) ? 1 : ((kCyNeg >> k & 1) ? -1 : 0);
             const int cls = (kCzPos >> k & 1) ? 0 : ((kCzNeg >> k & 1) ? 2 : 1);  // c_z +1, 0, -1
-            const int yr = wrap1(y0 - 2 + r, a.H);
-            const int xm = wrap1(x0 - SS::A + q * E, a.W);
+            const int yr = wrap1(y0 - 1 - cy + r, a.H);
+            const int xm = wrap1(x0 + x_0 + q * E, a.W);
             src[i] = reinterpret_cast<const char *>(a.src.f[k]) +
                      ((long)yr * a.W + xm) * (long)sizeof(S) + cls;
         }
@@ -145,14 +172,18 @@ struct StageCopy {
     }
 };
 
-// the 19 post-stream populations of the node at stage column col, row row
+// the 19 post-stream populations of the ring node (rx, ry) relative to the
+// tile origin (rx in -1..32, ry in -1..8): population k comes from row
+// ry - c_y (local row ry + 1 of its rows) and column rx - c_x
 template <typename S>
-__device__ __forceinline__ void pull_stage(const S *st, int col, int row, const float *wr,
+__device__ __forceinline__ void pull_stage(const S *st, int rx, int ry, const float *wr,
                                            float (&g)[19]) {
     using SS = StageShape<S>;
 #pragma unroll
     for (int k = 0; k < 19; k++)
-        g[k] = widen(st[k * SS::POP + (row - d3_cy(k)) * SS::RW + col - d3_cx(k)], wr[k]);
+        g[k] = widen(st[SS::first_chunk(k) * SS::E + (ry + 1) * SS::width(k) + rx - d3_cx(k) -
+                        SS::col0(k)],
+                     wr[k]);
 }
 
 __device__ __forceinline__ float psi_of(const D3Args &a, float rho) {
@@ -202,11 +233,11 @@ __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
         const bool ok = mbar_wait(&full[slot], (uint32_t)((j / SS::SLOTS) & 1), ST_WAIT);
         float(*ps)[ST_PX] = sp[(zs + 4) & 3];
         if (ok) {
-            pull_stage<S>(st, tx + SS::A, ty + 2, a.wr, gn);
+            pull_stage<S>(st, tx, ty, a.wr, gn);
             ps[ty + 1][tx + 1] = psi_of(a, d3q19_rho_native(gn));
             if (tid < ST_HALO) {
                 float gh[19];
-                pull_stage<S>(st, hx + SS::A, hy + 2, a.wr, gh);
+                pull_stage<S>(st, hx, hy, a.wr, gh);
                 ps[hy + 1][hx + 1] = psi_of(a, d3q19_rho_native(gh));
             }
         }
