@@ -76,8 +76,8 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
 // default up to TBLOCK_DEFAULT_MAX_NODES.  D3Q19 Shan-Chen without walls: the
 // staged single-pass step measured 28.6 / 34.1 / 34.2 GLUPS (FP32 / FP16 /
 // BF16) at 256^3 against 26.4 / 31.5 / 31.5 for the density pass + fused step
-// (28.8 / 35.6 / 35.7 with two steps per loop iteration and 3 blocks per SM
-// for 16-bit storage).
+// (32.9 / 38.9 / 39.0 with compact stages, two steps per loop iteration and
+// 3 blocks per SM).
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE | LB_TUNE_SC_STAGED;
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D2 = LB_TUNE_PDL;
 constexpr int TBLOCK_DEFAULT_SHAPE = 5;

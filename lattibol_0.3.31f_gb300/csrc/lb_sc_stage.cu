@@ -4,9 +4,10 @@
 //
 // A block of 256 threads owns a 32 x 8 column tile and marches through a
 // chunk of z planes.  The populations reach shared memory as "stages": stage
-// z holds, for every population k, the 12 rows y0-2 .. y0+9 of plane z - c_z(k)
-// over the columns x0-A .. x0+31+A (A = one 16-byte unit of elements), i.e.
-// everything the pull of plane z reads for the tile and two rings around it.
+// z holds, for every population k, exactly what the pulls of plane z read for
+// the tile and the ring around it -- rows y0-1-c_y .. y0+8-c_y of plane
+// z - c_z(k), columns x0-1-c_x .. x0+32-c_x rounded out to 16-byte chunks
+// (28.8 KB per FP32 stage, 16.6 KB per 16-bit stage: 3 blocks fit per SM).
 // The threads copy a stage in 16-byte cp.async chunks (each warp instruction
 // moves 512 contiguous bytes; periodic wrap is folded into each thread's chunk
 // addresses, formed once per block) and report on the slot's mbarrier when
