@@ -224,22 +224,39 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
     // 2^31 of them (the node count itself is below 2^31)
     const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
     const int nrows = nbx * a.H * a.D;
-    for (int r = blockIdx.x; r < nrows && ok; r += gridDim.x) {
+    // a run of 128 cells: this thread's cell, its flags and pulled populations
+    struct Run {
+        int o;
+        bool inside, fluid;
+        float g[19];
+    };
+    auto load = [&](int r, Run &u) {
         const int rr = a.reverse ? nrows - 1 - r : r;
         const int bx = rr % nbx, yz = rr / nbx;
         const int y = yz % a.H, z = yz / a.H;
         const int x = bx * D3_BLOCK + t;
-        const bool inside = x < a.W;
-        const int o = inside ? x + a.W * (y + a.H * z) : 0;
-        const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
-        const bool fluid = !(fl & CELL_WALL);
-        float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        u.inside = x < a.W;
+        u.o = u.inside ? x + a.W * (y + a.H * z) : 0;
+        const uint8_t fl = u.inside ? a.flags[u.o] : CELL_WALL;
+        u.fluid = !(fl & CELL_WALL);
+        if (u.fluid) {
+            const Nbr3 n(x, y, z, a.W, a.H, a.D);
+            pull_native<float>(a, u.o, n, fl, u.g);
+        }
+    };
+    // The next run's populations are loaded while this run's network runs on
+    // the tensor core: their DRAM latency overlaps the two MMAs and epilogues.
+    Run cur, nxt;
+    if (blockIdx.x < nrows) load(blockIdx.x, cur);
+    for (int r = blockIdx.x; r < nrows && ok; r += gridDim.x) {
+        const int o = cur.o;
+        const bool inside = cur.inside, fluid = cur.fluid;
+        float(&g)[19] = cur.g;
+        float rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
         float feat[MLP_IN];
 #pragma unroll
         for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
         if (fluid) {
-            const Nbr3 n(x, y, z, a.W, a.H, a.D);
-            pull_native<float>(a, o, n, fl, g);
             d3q19_moments_native(g, rho, ux, uy, uz);
             closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
         }
@@ -256,6 +273,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
             *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, 8 * h, MLP_IN_PAD)) =
                 *reinterpret_cast<const uint4 *>(p);
         }
+        if (r + (int)gridDim.x < nrows) load(r + gridDim.x, nxt);
         fence_proxy_async();
         tc_fence_before();
         __syncthreads();
@@ -320,27 +338,27 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         }
         yv = yv + ca.head_b3;
         tc_fence_before();  // the next run's MMA overwrites these columns after a barrier
-        if (!inside) continue;
-        if (!fluid) {
+        if (inside && !fluid) {
             if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
             if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
-            continue;
-        }
-        if (ca.y_out) ca.y_out[o] = yv;
-        const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
-        const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
-        if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
-        if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
-        float ex = ux, ey = uy, ez = uz;
-        if (a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
-            const float inv_rt = 1.f / (rho * tau_inv);
-            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
-            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
-            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
-        }
-        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
+        } else if (inside) {
+            if (ca.y_out) ca.y_out[o] = yv;
+            const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
+            const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
+            if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
+            if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
+            float ex = ux, ey = uy, ez = uz;
+            if (a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
+                const float inv_rt = 1.f / (rho * tau_inv);
+                if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
+                if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
+                if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
+            }
+            d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
 #pragma unroll
-        for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+            for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
+        }
+        cur = nxt;
     }
     if (!ok) {
         // an MMA did not complete: record it, give it one more bounded wait so
