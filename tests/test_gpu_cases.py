@@ -137,6 +137,12 @@ def lattice_cases(pkg):
     out.append(("d3q19_sc_bf16", dict(lattice=19, nx=24, ny=24, nz=24, tau_inv=1.0, G=-5.0,
                                       storage=a.LB_STORE_BF16, rho_ref=0.693),
                 np.zeros(n, np.uint8), rho))
+    # D3Q19 Shan-Chen FP32 on a wall-free lattice the staged single-pass step tiles
+    n3 = 32 * 16 * 12
+    rho3 = (0.693 * (1 + 0.01 * (2 * rng.random(n3) - 1))).astype(np.float32)
+    out.append(("d3q19_sc_staged_f32", dict(lattice=19, nx=32, ny=16, nz=12, tau_inv=1.0,
+                                            G=-5.0, force=(1e-6, 0, 0)),
+                np.zeros(n3, np.uint8), rho3))
     # D2Q9 in the reference's semantics: Zou-He, solids, Shan-Chen
     W2, H2 = 48, 32
     sol = (rng.random((H2, W2)) < 0.08).astype(np.uint8)
@@ -156,8 +162,8 @@ def build(pkg, kw, flags, rho):
     return lat
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2], ids=["d3q19_native_f32", "d3q19_sc_bf16",
-                                                "d2q9_reference_sc"])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3], ids=["d3q19_native_f32", "d3q19_sc_bf16",
+                                                   "d3q19_sc_staged_f32", "d2q9_reference_sc"])
 def test_checkpoint_resume_is_bit_identical(pkg, tmp_path, idx):
     name, kw, flags, rho = lattice_cases(pkg)[idx]
     K = 9

@@ -65,6 +65,10 @@ CASES = {
                         (0, 9, 4), 13),
     "d3q19_shan_chen_bf16": (19, (24, 24, 24), dict(tau_inv=1.0, G=-5.0, storage=2,
                                                     rho_ref=0.693), (3, 5, 7), 11),
+    # wall-free lattices that the staged single-pass Shan-Chen step tiles
+    "d3q19_shan_chen_staged_f16": (19, (32, 16, 12), dict(tau_inv=1.0, G=-5.0, storage=1,
+                                                          rho_ref=0.693), (31, 15, 11), 11),
+    "d3q19_shan_chen_staged_f32": (19, (64, 8, 8), dict(tau_inv=1.0, G=-5.0), (5, 3, 2), 13),
     "d2q9_pdl": (9, (72, 40, 1), dict(tau_inv=1.6, wall_u=(0.1, 0, 0)), (30, 1, 0), 70),
     "d2q9_persistent": (9, (72, 40, 1), dict(tau_inv=1.6, wall_u=(0.1, 0, 0), tuning=0x104),
                         (30, 1, 0), 70),
