@@ -312,8 +312,10 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_march_kernel(cons
 // (cp.async.wait_group) and a warp barrier makes every lane's copies visible;
 // no block barrier.  An item qualifies when its domain's rows start on 16
 // bytes and no chunk straddles its periodic x edge (W a multiple of 32, first
-// node a multiple of 4); other items take the plain march.  Same pulls and
-// arithmetic as the march, so the same bits.
+// node a multiple of 4); the work list puts those first, and the other items
+// take the plain march in a second launch (kept out of this kernel, whose
+// registers it would crowd).  Same pulls and arithmetic as the march, so the
+// same bits.
 // ---------------------------------------------------------------------------
 constexpr int ENS_RING = 6;                    // source-row slots per warp
 constexpr int ENS_RCOLS = ET_BX + 8;           // columns x0 - 4 .. x0 + 35
@@ -347,10 +349,7 @@ __global__ void __launch_bounds__(ENS_MARCH_THREADS, MINB) ens_ring_kernel(const
     const int col = 4 + lane, hcol = lane == 0 ? 3 : 4 + ET_BX;  // ring columns of x, xh
     for (int it = blockIdx.x * warps_per_block + warp; it < a.nitems; it += nwarps) {
         const EnsItem dm = a.items[it];
-        if ((dm.W & 31) || (dm.off & 3)) {
-            ens_march_item<R, MOM>(a, dm, lane);
-            continue;
-        }
+        if ((dm.W & 31) || (dm.off & 3)) continue;  // the work list gives this kernel none
         const int y_end = min(dm.y + R, dm.H);
         const bool small_h = dm.H < 4;
         // this lane's chunks of a source row (chunk c = 10 k + q: population k,
@@ -529,6 +528,7 @@ struct lb_ensemble {
     float *psi = nullptr, *mom = nullptr;
     EnsItem *items_d = nullptr;
     int nitems = 0, items_cap = 0;
+    int nring = 0;  // ring strip shapes: the leading items the ring kernel takes
     int cur = 0, psi_form = LB_PSI_EXP1, sms = 1, graph_steps = 32;
     // single-pass warp strips of 32 rows with the shared-memory row ring, 3
     // blocks per SM: 72.4 GLUPS on 512 droplet domains, against 63.2 for the
@@ -573,7 +573,37 @@ EnsArgs args_for(lb_ensemble *e, int from) {
     return a;
 }
 
-int launches_per_step(const lb_ensemble *e) { return e->shape.bx == 0 ? 1 : 2; }
+int launches_per_step(const lb_ensemble *e) {
+    if (e->shape.bx != 0) return 2;
+    if (ens_ring_rows(e->shape.ry)) return (e->nring > 0) + (e->nitems > e->nring);
+    return 1;
+}
+
+// ring strip shapes: the ring kernel over the leading qualifying items, the
+// plain march over the rest
+template <int R, int MINB>
+cudaError_t ens_ring_step(lb_ensemble *e, const EnsArgs &a, bool mom) {
+    const auto grid_for = [e](int n) {
+        return (unsigned)std::max(1, std::min(n, e->sms * e->shape.bps));
+    };
+    EnsArgs ar = a, am = a;
+    ar.nitems = e->nring;
+    am.items = a.items + e->nring;
+    am.nitems = a.nitems - e->nring;
+    if (ar.nitems > 0) {
+        const cudaError_t c = ens_ring_launch<R, MINB>(ar, mom, grid_for(ar.nitems), e->stream);
+        if (c != cudaSuccess) return c;
+        e->launches += 1;
+    }
+    if (am.nitems > 0) {
+        const unsigned g = grid_for(am.nitems);
+        if (mom) ens_march_kernel<R, MINB, true><<<g, ENS_MARCH_THREADS, 0, e->stream>>>(am);
+        else ens_march_kernel<R, MINB, false><<<g, ENS_MARCH_THREADS, 0, e->stream>>>(am);
+        e->launches += 1;
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
+}
 
 cudaError_t ens_step(lb_ensemble *e, int from, bool mom) {
     const EnsArgs a = args_for(e, from);
@@ -595,11 +625,8 @@ cudaError_t ens_step(lb_ensemble *e, int from, bool mom) {
             LB_ENS_MARCH(LB_ENS_MLAUNCH)
 #undef LB_ENS_MLAUNCH
 #define LB_ENS_RLAUNCH(S, R, MINB)                                                             \
-    case S: {                                                                                  \
-        const cudaError_t c = ens_ring_launch<R, MINB>(a, mom, grid, e->stream);               \
-        if (c != cudaSuccess) return c;                                                        \
-        break;                                                                                 \
-    }
+    case S:                                                                                    \
+        return ens_ring_step<R, MINB>(e, a, mom);
             LB_ENS_RING(LB_ENS_RLAUNCH)
 #undef LB_ENS_RLAUNCH
             default: return cudaErrorInvalidValue;
@@ -627,20 +654,25 @@ void drop_graphs(lb_ensemble *e) {
 
 // work list of row groups for the current shape
 int build_items(lb_ensemble *e) {
-    std::vector<EnsItem> items;
+    std::vector<EnsItem> items, rest;
     for (int d = 0; d < e->nd; d++) {
         const EnsDomain &m = e->dom[d];
         if (e->shape.bx == 0) {  // tiles or strips, row by row
             const int rows = ens_tile_rows(e->shape.ry) + ens_march_rows(e->shape.ry) +
                              ens_ring_rows(e->shape.ry);
+            // ring strips: the items the ring kernel takes first, the rest after
+            const bool ring = ens_ring_rows(e->shape.ry) > 0;
+            std::vector<EnsItem> &to = ring && ((m.W & 31) || (m.off & 3)) ? rest : items;
             for (int y = 0; y < m.H; y += rows)
                 for (int x = 0; x < m.W; x += ET_BX)
-                    items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, x});
+                    to.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, x});
         } else {  // groups of ry rows
             for (int y = 0; y < m.H; y += e->shape.ry)
                 items.push_back(EnsItem{m.off, m.W, m.H, y, m.G, m.tau_inv, 0});
         }
     }
+    e->nring = (int)items.size();
+    items.insert(items.end(), rest.begin(), rest.end());
     if ((int)items.size() > e->items_cap) {
         if (e->items_d) cudaFree(e->items_d);
         e->items_d = nullptr;
