@@ -187,13 +187,17 @@ __device__ __forceinline__ void pull_stage(const S *st, int rx, int ry, const fl
                      wr[k]);
 }
 
-__device__ __forceinline__ float psi_of(const D3Args &a, float rho) {
-    return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
+// the pseudo-potential of the configured form (LB_PSI_REF = 0: the
+// reference's 4 exp(-200/rho); LB_PSI_EXP1: 1 - exp(-rho)), a compile-time
+// choice so that each kernel carries the code of one form only
+template <int PSI>
+__device__ __forceinline__ float psi_of(float rho) {
+    return PSI == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
 }  // namespace
 
-template <typename S, bool MOM>
+template <typename S, bool MOM, int PSI>
 __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
     d3q19_sc_stage_kernel(const __grid_constant__ D3Args a, int zc) {
     using SS = StageShape<S>;
@@ -235,11 +239,11 @@ __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
         float(*ps)[ST_PX] = sp[(zs + 4) & 3];
         if (ok) {
             pull_stage<S>(st, tx, ty, a.wr, gn);
-            ps[ty + 1][tx + 1] = psi_of(a, d3q19_rho_native(gn));
+            ps[ty + 1][tx + 1] = psi_of<PSI>(d3q19_rho_native(gn));
             if (tid < ST_HALO) {
                 float gh[19];
                 pull_stage<S>(st, hx, hy, a.wr, gh);
-                ps[hy + 1][hx + 1] = psi_of(a, d3q19_rho_native(gh));
+                ps[hy + 1][hx + 1] = psi_of<PSI>(d3q19_rho_native(gh));
             }
         }
         if (__syncthreads_or(!ok)) {
@@ -311,21 +315,24 @@ int sc_stage_chunk(int W, int H, int D) {
 
 namespace {
 
-template <typename S>
-cudaError_t stage_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
+template <typename S, bool MOM, int PSI>
+cudaError_t stage_launch(const D3Args &a, int zc, cudaStream_t s) {
     using SS = StageShape<S>;
     static_assert(SS::MIN_BLOCKS * (SS::SMEM + 1024) <= 228 * 1024, "resident blocks per SM");
     // once per instantiation
-    static const cudaError_t attr_e[2] = {
-        cudaFuncSetAttribute(d3q19_sc_stage_kernel<S, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM),
-        cudaFuncSetAttribute(d3q19_sc_stage_kernel<S, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM)};
-    if (attr_e[mom ? 1 : 0] != cudaSuccess) return attr_e[mom ? 1 : 0];
+    static const cudaError_t attr_e = cudaFuncSetAttribute(
+        d3q19_sc_stage_kernel<S, MOM, PSI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM);
+    if (attr_e != cudaSuccess) return attr_e;
     const dim3 g(a.W / ST_TX, a.H / ST_TY, a.D / zc);
-    if (mom) d3q19_sc_stage_kernel<S, true><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
-    else d3q19_sc_stage_kernel<S, false><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
+    d3q19_sc_stage_kernel<S, MOM, PSI><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
     return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t stage_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
+    if (a.psi_form == 0)
+        return mom ? stage_launch<S, true, 0>(a, zc, s) : stage_launch<S, false, 0>(a, zc, s);
+    return mom ? stage_launch<S, true, 1>(a, zc, s) : stage_launch<S, false, 1>(a, zc, s);
 }
 
 }  // namespace

@@ -105,6 +105,35 @@ def test_staged_vs_oracle(pkg, oracle, storage):
     assert beq(rho_g, mom[3]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1]) and beq(uz_g, mom[2])
 
 
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_staged_reference_psi_matches_two_pass(pkg, storage):
+    """The reference's pseudo-potential psi = 4 exp(-200/rho) (rho near 200,
+    G = -120, as in the reference's Shan-Chen samples) through the staged
+    step, bit-exact against the two-pass step."""
+    W, H, D = 64, 16, 12
+    N = W * H * D
+    rng = np.random.default_rng(9)
+    rho = (200.0 * (1 + rng.uniform(-0.01, 0.01, N))).astype(np.float32)
+    z = np.zeros(N, np.float32)
+    out = []
+    for tuning in (STAGED, TWO_PASS):
+        lat = pkg.Lattice(19, W, H, D, tau_inv=1.0, G=-120.0, psi_form=pkg.abi.LB_PSI_REF,
+                          storage=storage, rho_ref=200.0, tuning=tuning, graph_steps=4)
+        lat.set_flags(np.zeros(N, np.uint8))
+        lat.init_equilibrium(rho, z, z, z)
+        b = lat.launches()
+        lat.step(10)
+        n = lat.launches() - b  # before populations(): 16-bit reads launch conversions
+        out.append((lat.populations(), lat.moments(), n))
+        lat.close()
+    (f_s, m_s, l_s), (f_t, m_t, l_t) = out
+    assert l_s == 10 and l_t == 20
+    assert np.isfinite(f_s).all()
+    assert beq(f_s, f_t)
+    for a, b in zip(m_s, m_t):
+        assert beq(a, b)
+
+
 def test_walls_take_the_two_pass_step(pkg):
     W, H, D = 64, 16, 16
     N = W * H * D
