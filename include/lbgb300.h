@@ -347,8 +347,10 @@ int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **u
 int lb_tcgen05_selftest(float *out, int *status);
 /* self-check of the bounded waits on the GPU: which = 0 makes the persistent
  * D2Q9 loop's band wait run out (a counter that nothing raises), which = 1 the
- * tcgen05 kernels' mbarrier wait (nothing committed).  *status = 1 when the
- * wait gave up as designed, reported the failure and returned. */
+ * tcgen05 kernels' mbarrier wait (nothing committed), which = 2 the staged
+ * Shan-Chen step's stage wait (given no polls; the block then waits for the
+ * copies it issued before it returns).  *status = 1 when the wait gave up as
+ * designed, reported the failure and returned. */
 int lb_wait_selftest(int which, int *status);
 int lb_extents(const lb_ctx *ctx, int *nx, int *ny, int *nz);
 

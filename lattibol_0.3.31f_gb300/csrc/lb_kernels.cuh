@@ -65,6 +65,9 @@ cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaSt
 // sets *a.err (when a.err is set).
 int sc_stage_chunk(int W, int H, int D);
 cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom, cudaStream_t s);
+// self-check of the staged step's bounded wait: one block whose first stage
+// waits get no polls gives up, sets *err (device memory) and returns
+cudaError_t sc_stage_wait_selftest(int *err);
 // equilibrium written in 16-bit deviation storage (storage 1 or 2; Pop holds
 // the storage arrays reinterpreted as float*)
 cudaError_t launch_d3q19_equilibrium_storage(const Pop<19> &p, const float *rho, const float *ux,

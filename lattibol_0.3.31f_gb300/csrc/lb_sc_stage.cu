@@ -32,9 +32,11 @@
 // d3q19_sc_sum_native, d3q19_bgk_native), so the result is bit-identical to
 // the density pass + fused step.
 //
-// Every mbarrier wait is bounded; a block that gives up raises the device
-// error word, waits (bounded) for the copies it still has in flight and
-// returns.  (A first form copied each stage row with one cp.async.bulk per
+// Every mbarrier wait is bounded (wait_limit polls of about a microsecond for
+// a stage; ST_WAIT in the library's launches); a block that gives up raises
+// the device error word, waits (bounded by ST_WAIT) for the copies it still
+// has in flight and returns.  sc_stage_wait_selftest makes the first wait run
+// out (wait_limit 0) to exercise that path.  (A first form copied each stage row with one cp.async.bulk per
 // population and row, 228 copies per stage: 20.9 GLUPS for FP32 and 16-bit
 // alike at 256^3, bound by the number of copies, not their bytes.)
 #include <cuda_bf16.h>
@@ -199,7 +201,7 @@ __device__ __forceinline__ float psi_of(float rho) {
 
 template <typename S, bool MOM, int PSI>
 __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
-    d3q19_sc_stage_kernel(const __grid_constant__ D3Args a, int zc) {
+    d3q19_sc_stage_kernel(const __grid_constant__ D3Args a, int zc, int wait_limit) {
     using SS = StageShape<S>;
     extern __shared__ __align__(128) unsigned char smem[];
     S *stage = reinterpret_cast<S *>(smem);
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
         const int slot = j % SS::SLOTS;
         const int zs = z0 - 1 + j;
         const S *st = stage + slot * SS::ELEMS;
-        const bool ok = mbar_wait(&full[slot], (uint32_t)((j / SS::SLOTS) & 1), ST_WAIT);
+        const bool ok = mbar_wait(&full[slot], (uint32_t)((j / SS::SLOTS) & 1), wait_limit);
         float(*ps)[ST_PX] = sp[(zs + 4) & 3];
         if (ok) {
             pull_stage<S>(st, tx, ty, a.wr, gn);
@@ -324,7 +326,7 @@ cudaError_t stage_launch(const D3Args &a, int zc, cudaStream_t s) {
         d3q19_sc_stage_kernel<S, MOM, PSI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS::SMEM);
     if (attr_e != cudaSuccess) return attr_e;
     const dim3 g(a.W / ST_TX, a.H / ST_TY, a.D / zc);
-    d3q19_sc_stage_kernel<S, MOM, PSI><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc);
+    d3q19_sc_stage_kernel<S, MOM, PSI><<<g, ST_THREADS, SS::SMEM, s>>>(a, zc, ST_WAIT);
     return cudaGetLastError();
 }
 
@@ -336,6 +338,37 @@ cudaError_t stage_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
 }
 
 }  // namespace
+
+// The give-up path of the staged step on a 32 x 8 x 4 FP32 lattice: every
+// first stage wait is given no polls, so each block reports through *err,
+// waits for the stages its prologue issued and returns.
+cudaError_t sc_stage_wait_selftest(int *err) {
+    constexpr int W = ST_TX, H = ST_TY, D = 4, N = W * H * D;
+    using SS = StageShape<float>;
+    float *buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, sizeof(float) * 2 * 19 * N);
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(buf, 0, sizeof(float) * 2 * 19 * N);
+    D3Args a{};
+    for (int k = 0; k < 19; k++) {
+        a.src.f[k] = buf + (long)k * N;
+        a.dst.f[k] = buf + (long)(19 + k) * N;
+    }
+    a.W = W; a.H = H; a.D = D; a.ndev = 1;
+    a.tau_inv = 1.f; a.G = -5.f; a.psi_form = 1;
+    a.err = err;
+    static const cudaError_t attr_e = cudaFuncSetAttribute(
+        d3q19_sc_stage_kernel<float, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SS::SMEM);
+    if (e == cudaSuccess) e = attr_e;
+    if (e == cudaSuccess) {
+        d3q19_sc_stage_kernel<float, false, 1><<<dim3(1, 1, 1), ST_THREADS, SS::SMEM>>>(a, D, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(buf);
+    return e;
+}
 
 cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom, cudaStream_t s) {
     const int zc = sc_stage_chunk(a.W, a.H, a.D);
