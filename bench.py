@@ -61,7 +61,7 @@ class Workload:
 
     def flags(self):
         nx, ny, nz = self.size
-        if self.name == "channel":
+        if self.name.startswith("channel"):
             fl = np.zeros((nz, ny, nx), np.uint8)
             fl[:, 0, :] = fl[:, -1, :] = 1
             fl[0, :, :] = fl[-1, :, :] = 1
@@ -106,6 +106,17 @@ WORKLOADS = {
                         "(32x14 tiles with their halo in shared memory), graph-replayed "
                         "programmatic dependent launches"}),
 }
+# the channel with 16-bit deviation storage (f_k - w_k * 1.0 kept in binary16 /
+# bfloat16, FP32 arithmetic): 19x2 loads + 19x2 stores + 1 flag byte per update
+for _st, _nm in [(1, "f16"), (2, "bf16")]:
+    WORKLOADS["channel_" + _nm] = Workload(
+        "channel_" + _nm, 19, (256, 128, 128), 0.55, 20000, 2 * 19 * 2 + 1,
+        force=(1e-6, 0, 0), storage=_st, rho_ref=1.0, dtype=_nm,
+        describe={"body_force_x": 1e-6, "sphere": {"center": [64, 64, 64], "radius": 16},
+                  "boundaries": "x periodic, half-way bounce-back on y/z faces and sphere",
+                  "init": "equilibrium rho=1 u=0", "storage": _nm,
+                  "storage_offset": "f_k - w_k*1.0",
+                  "l2": "state (0.64 GB) larger than L2"})
 # D3Q19 Shan-Chen spinodal decomposition, 256^3 periodic, tau = 1, G = -5,
 # psi = 1 - exp(-rho); algorithmic bytes/LU: populations read + written once,
 # 152 (FP32) / 76 (16-bit deviation storage).  The default step (single pass,

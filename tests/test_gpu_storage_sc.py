@@ -194,6 +194,56 @@ def test_spinodal_error_vs_fp64(pkg, oracle):
         assert v["mass_drift"] < {"f32": 5e-5, "f16": 1e-3, "bf16": 1e-2}[name], (key, v)
 
 
+def test_channel_storage_error_vs_fp64(pkg, oracle):
+    """Error statement for the channel past a sphere with 16-bit deviation
+    storage (f_k - w_k, rho_ref = 1): a 64x32x32 channel (y/z walls, sphere of
+    radius 4, tau = 0.55, g_x = 1e-5) run 1000 steps in FP32, FP16 and BF16
+    storage against the FP64 oracle.  Reported: max |rho - rho64|, |u -
+    u64|_2 / |u64|_2 and the relative kinetic-energy error.  Bounds (loose;
+    the printed figures are the statement): u error 1e-4 (FP32), 2e-2
+    (FP16), 2e-1 (BF16)."""
+    W, H, D, steps = 64, 32, 32, 1000
+    N = W * H * D
+    fl = np.zeros((D, H, W), np.uint8)
+    fl[:, 0, :] = fl[:, -1, :] = 1
+    fl[0, :, :] = fl[-1, :, :] = 1
+    z, y, x = np.mgrid[0:D, 0:H, 0:W]
+    fl[(x - 16) ** 2 + (y - 16) ** 2 + (z - 16) ** 2 <= 16] = 1
+    flags = fl.reshape(-1)
+    fluid = flags == 0
+    tau_inv = 1 / 0.55
+    F = (1e-5, 0.0, 0.0)
+    one = np.ones(N)
+    f64 = oracle.d3q19_equilibrium(one, np.zeros(N), np.zeros(N), np.zeros(N),
+                                   1 / 3, 1 / 18, 1 / 36)
+    mom64 = [np.zeros(N) for _ in range(4)]
+    zc = np.zeros(19)
+    for _ in range(steps):
+        oracle.d3q19_stream_native(f64, flags, zc, W, H, D)
+        oracle.d3q19_collide_native(f64, flags, mom64, W, H, D, 1 / 3, 1 / 18, 1 / 36, tau_inv,
+                                    F)
+    ux64, uy64, uz64, rho64 = (m[fluid] for m in mom64)
+    u64 = np.stack([ux64, uy64, uz64])
+    ke64 = float(np.sum(rho64 * np.sum(u64 ** 2, axis=0)))
+    report = {}
+    for storage, name in [(0, "f32"), (1, "f16"), (2, "bf16")]:
+        lat = pkg.Lattice(19, W, H, D, tau_inv=np.float32(tau_inv),
+                          force=tuple(np.float32(v) for v in F), storage=storage, rho_ref=1.0)
+        lat.set_flags(flags)
+        lat.init_equilibrium(np.ones(N, np.float32), None, None, None)
+        lat.step(steps)
+        rho, ux, uy, uz = (m[fluid].astype(np.float64) for m in lat.moments())
+        lat.close()
+        u = np.stack([ux, uy, uz])
+        ke = float(np.sum(rho * np.sum(u ** 2, axis=0)))
+        report[name] = {"rho_max_err": float(np.max(np.abs(rho - rho64))),
+                        "u_err": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
+                        "ke_err": abs(ke - ke64) / ke64}
+    print("CHANNEL_ERRORS 64x32x32, 1000 steps, vs FP64 oracle: %s" % report)
+    for name, bound in [("f32", 1e-4), ("f16", 2e-2), ("bf16", 2e-1)]:
+        assert report[name]["u_err"] < bound, (name, report[name])
+
+
 @pytest.mark.parametrize("tuning", [0x102, 0x100], ids=["single_pass", "two_pass"])
 @pytest.mark.parametrize("storage", [0, 2], ids=["f32", "bf16"])
 def test_shan_chen_paths_with_walls_vs_oracle(pkg, oracle, tuning, storage):
