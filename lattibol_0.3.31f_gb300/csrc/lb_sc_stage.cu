@@ -302,8 +302,10 @@ __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
 }
 
 // z-chunk of the staged kernel, 0 if the lattice does not tile: the longest
-// march that still gives at least 1216 blocks (four waves of 2 blocks on 152
-// SMs), else the shortest that divides D
+// march that still gives at least 1216 blocks (eight per SM on 152 SMs, about
+// three waves of 3 resident blocks), else the shortest that divides D.  At
+// 256^3 that is 32 planes (2048 blocks); 16 planes measured slower (more
+// halo planes per plane).
 int sc_stage_chunk(int W, int H, int D) {
     if (W % ST_TX || H % ST_TY) return 0;
     int pick = 0;
