@@ -304,7 +304,9 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int q = 8 * h + 2 * j;
-                    p[j] = bf16x2_relu(v[q] + ca.head_b1[c + q], v[q + 1] + ca.head_b1[c + q + 1]);
+                    const float2 h = __fadd2_rn(make_float2(v[q], v[q + 1]),
+                                                make_float2(ca.head_b1[c + q], ca.head_b1[c + q + 1]));
+                    p[j] = bf16x2_relu(h.x, h.y);
                 }
                 *reinterpret_cast<uint4 *>(sm.a + kmajor_offset(t, c + 8 * h, MLP_H)) =
                     make_uint4(p[0], p[1], p[2], p[3]);
@@ -326,17 +328,23 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        // 5. output: b3 + sum_j w3_j ReLU(D_j + b2_j)
-        float yv = 0.f;
+        // 5. output: b3 + sum_j w3_j ReLU(D_j + b2_j), even and odd j in the two
+        // lanes of paired FP32 instructions (two accumulation chains)
+        float2 y2 = make_float2(0.f, 0.f);
 #pragma unroll
         for (int c = 0; c < MLP_H; c += 32) {
             float v[32];
             tc_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
-            for (int j = 0; j < 32; j++)
-                yv = __fmaf_rn(ca.head_w3[c + j], fmaxf(v[j] + ca.head_b2[c + j], 0.f), yv);
+            for (int j = 0; j < 32; j += 2) {
+                float2 h = __fadd2_rn(make_float2(v[j], v[j + 1]),
+                                      make_float2(ca.head_b2[c + j], ca.head_b2[c + j + 1]));
+                h.x = fmaxf(h.x, 0.f);
+                h.y = fmaxf(h.y, 0.f);
+                y2 = __ffma2_rn(make_float2(ca.head_w3[c + j], ca.head_w3[c + j + 1]), h, y2);
+            }
         }
-        yv = yv + ca.head_b3;
+        const float yv = (y2.x + y2.y) + ca.head_b3;
         tc_fence_before();  // the next run's MMA overwrites these columns after a barrier
         if (inside && !fluid) {
             if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
