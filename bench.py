@@ -531,6 +531,10 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    # the same rate counted over fluid nodes only (wall nodes move no data)
+    n_fluid = int(np.count_nonzero((flags & 1) == 0))
+    line["fluid_nodes"] = n_fluid
+    line["fluid_glups"] = glups * n_fluid / N
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline and ws == 1:
