@@ -76,8 +76,8 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
 // default up to TBLOCK_DEFAULT_MAX_NODES.  D3Q19 Shan-Chen without walls: the
 // staged single-pass step measured 28.6 / 34.1 / 34.2 GLUPS (FP32 / FP16 /
 // BF16) at 256^3 against 26.4 / 31.5 / 31.5 for the density pass + fused step
-// (32.9 / 38.9 / 39.0 with compact stages, two steps per loop iteration and
-// 3 blocks per SM).
+// (34.9 / 40.3 / 40.4 with compact stages, two steps per loop iteration, 3
+// blocks per SM and 32-bit chunk offsets).
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D3 = LB_TUNE_REVERSE | LB_TUNE_SC_STAGED;
 constexpr int LB_TUNE_LIBRARY_DEFAULT_D2 = LB_TUNE_PDL;
 constexpr int TBLOCK_DEFAULT_SHAPE = 5;
@@ -133,8 +133,11 @@ bool sc_on(const lb_ctx *c) {
 // asynchronous copies: native mode, no wall node, a lattice it tiles, and the
 // tuning asks for it
 bool sc_stage_on(const lb_ctx *c) {
+    // (the kernel addresses the populations as 32-bit element offsets from the
+    // first array: all 19 must lie within 2^32 elements of it)
     return c->Q == 19 && c->cfg.mode == LB_MODE_NATIVE && sc_on(c) && !c->any_wall &&
-           (c->tune & LB_TUNE_SC_STAGED) && sc_stage_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz);
+           (c->tune & LB_TUNE_SC_STAGED) && sc_stage_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz) &&
+           19L * c->stride < (1L << 32);
 }
 
 // the D2Q9 persistent step loop applies: no Shan-Chen pass and the tuning

@@ -122,18 +122,22 @@ constexpr unsigned kCyPos = cy_mask(1), kCyNeg = cy_mask(-1);
 // A stage is copied in 16-byte chunks: chunk c of a slot is bytes 16c .. 16c+15,
 // element (k, row, col) of the stage layout.  Thread t copies chunks t, t + 256,
 // ...; which global row and column each of its chunks reads does not change
-// from plane to plane, so the thread forms those addresses once (for plane 0,
+// from plane to plane, so the thread forms those offsets once: the element
+// offset from population 0's array in plane 0 (the populations lie at
+// f[0] + k * stride, and the launch guarantees 19 strides fit in 32 bits),
 // with the chunk's z class -- plane z - c_z read for plane z -- in the two low
-// bits, free because every chunk address is 16-byte aligned).
+// bits, free because every chunk starts on a 16-byte boundary.
 template <typename S>
 struct StageCopy {
     using SS = StageShape<S>;
     static constexpr int E = SS::E;
     static constexpr int CHUNKS = SS::CHUNKS;
     static constexpr int PER_T = (CHUNKS + ST_THREADS - 1) / ST_THREADS;  // 8 / 5
-    const char *src[PER_T];
+    uint32_t off[PER_T];
 
     __device__ __forceinline__ StageCopy(const D3Args &a, int x0, int y0) {
+        const long stride = (reinterpret_cast<const char *>(a.src.f[1]) -
+                             reinterpret_cast<const char *>(a.src.f[0])) / (long)sizeof(S);
 #pragma unroll
         for (int i = 0; i < PER_T; i++) {
             const int c = min((int)threadIdx.x + ST_THREADS * i, CHUNKS - 1);
@@ -152,24 +156,24 @@ struct StageCopy {
             const int cls = (kCzPos >> k & 1) ? 0 : ((kCzNeg >> k & 1) ? 2 : 1);  // c_z +1, 0, -1
             const int yr = wrap1(y0 - 1 - cy + r, a.H);
             const int xm = wrap1(x0 + x_0 + q * E, a.W);
-            src[i] = reinterpret_cast<const char *>(a.src.f[k]) +
-                     ((long)yr * a.W + xm) * (long)sizeof(S) + cls;
+            off[i] = (uint32_t)(k * stride + (long)yr * a.W + xm) | (uint32_t)cls;
         }
     }
 
     // stage of plane zs into slot; one arrival per thread on mbar
     __device__ __forceinline__ void issue(const D3Args &a, S *slot, uint64_t *mbar, int zs) const {
-        const long plane = (long)a.W * a.H * (long)sizeof(S);
-        // byte offset of the plane read by each z class, minus the class tag
-        const long o0 = wrap1(zs - 1, a.D) * plane, o1 = wrap1(zs, a.D) * plane - 1,
-                   o2 = wrap1(zs + 1, a.D) * plane - 2;
+        const S *base = reinterpret_cast<const S *>(a.src.f[0]);
+        const uint32_t plane = (uint32_t)a.W * (uint32_t)a.H;
+        // element offset of the plane read by each z class, minus the class tag
+        const uint32_t o0 = (uint32_t)wrap1(zs - 1, a.D) * plane,
+                       o1 = (uint32_t)wrap1(zs, a.D) * plane - 1u,
+                       o2 = (uint32_t)wrap1(zs + 1, a.D) * plane - 2u;
         char *dst = reinterpret_cast<char *>(slot) + 16 * threadIdx.x;
 #pragma unroll
         for (int i = 0; i < PER_T; i++) {
             if (i == PER_T - 1 && (int)threadIdx.x + ST_THREADS * i >= CHUNKS) break;
-            const char *p = src[i];
-            const int cls = (int)(reinterpret_cast<uintptr_t>(p) & 3);
-            cp16(dst + 16 * ST_THREADS * i, p + (cls == 0 ? o0 : (cls == 1 ? o1 : o2)));
+            const uint32_t e = off[i], cls = e & 3u;
+            cp16(dst + 16 * ST_THREADS * i, base + (e + (cls == 0 ? o0 : (cls == 1 ? o1 : o2))));
         }
         cp_arrive(mbar);
     }
