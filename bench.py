@@ -90,10 +90,11 @@ WORKLOADS = {
     # 19x4 loads + 19x4 stores + 1 flag byte (moments only on the last step)
     "channel": Workload(
         "channel", 19, (256, 128, 128), 0.55, 20000, 2 * 19 * 4 + 1, force=(1e-6, 0, 0),
-        # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-        # the ncu capture in profiles/d3q19_fused_channel_256x128x128.md (captured at
-        # 128^3 and scaled by the node count to this lattice)
-        traffic=522.1e6, profile="profiles/d3q19_fused_channel_256x128x128.md",
+        # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum),
+        # captured on this lattice with the caches left as the previous step
+        # left them (ncu --cache-control none, mean of two launches; the
+        # capture is in profiles/d3q19_fused_channel_256x128x128.md)
+        traffic=578.4e6, profile="profiles/d3q19_fused_channel_256x128x128.md",
         describe={"body_force_x": 1e-6, "sphere": {"center": [64, 64, 64], "radius": 16},
                   "boundaries": "x periodic, half-way bounce-back on y/z faces and sphere",
                   "init": "equilibrium rho=1 u=0",
@@ -450,6 +451,8 @@ def main():
     ap.add_argument("--workload", default="channel",
                     choices=sorted(WORKLOADS) + ["ensemble", "closure"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-f16", action="store_true",
+                    help="channel: skip the 16-bit storage figure beside the FP32 one")
     ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--tuning", type=lambda v: int(v, 0), default=0,
                     help="lb_config.tuning (0 = the library's default)")
@@ -510,6 +513,11 @@ def main():
     assert np.isfinite(mom[0]).all() and np.isfinite(mom[1]).all()
     lat.close()
 
+    # ------------------------- the same lattice with 16-bit deviation storage
+    f16 = None
+    if wl.name == "channel" and not args.no_f16:
+        f16 = measure_f16(pkg, wl, flags, args, ws, dist, glups)
+
     # ------------------------------------------------ end to end through the C ABI
     e2e = None
     if args.e2e_steps > 0 and wl.name == "channel":
@@ -535,6 +543,8 @@ def main():
     n_fluid = int(np.count_nonzero((flags & 1) == 0))
     line["fluid_nodes"] = n_fluid
     line["fluid_glups"] = glups * n_fluid / N
+    if f16:
+        line["fp16_storage"] = f16
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline and ws == 1:
@@ -542,6 +552,37 @@ def main():
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     return 0
+
+
+def measure_f16(pkg, wl, flags, args, ws, dist, glups_f32):
+    """The headline lattice again with populations stored as binary16
+    deviations f_k - w_k (FP32 arithmetic), same physics, steps and timing:
+    the "FP16-store vs FP32" figure of the metric.  Its roofline counts
+    19 x 2 loads + 19 x 2 stores + 1 flag byte = 77 B per update."""
+    nx, ny, nz = wl.size
+    lat = pkg.Lattice(wl.lattice, nx, ny, nz, tau_inv=np.float32(1 / wl.tau),
+                      force=tuple(np.float32(v) for v in wl.force), wall_u=wl.wall_u,
+                      graph_steps=args.graph_steps, tuning=args.tuning, storage=1, rho_ref=1.0)
+    lat.set_flags(flags)
+    lat.init_equilibrium(None)
+    lat.step(args.warmup)
+    lat.synchronize()
+    if dist:
+        dist.barrier()
+    n0 = lat.launches()
+    ms = lat.time_steps(args.steps)
+    launches = lat.launches() - n0
+    assert np.isfinite(lat.moments()[0]).all()
+    lat.close()
+    ms = dist_max(dist, ms)
+    glups = ws * wl.N * args.steps / (ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    achieved = 77 * wl.N / (ms / args.steps * 1e-3) / 1e9
+    return {"value": glups, "unit": "GLUPS", "ms_per_step": ms / args.steps,
+            "vs_fp32": glups / glups_f32, "storage": "binary16 f_k - w_k*1.0, FP32 arithmetic",
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "bytes_per_lu": 77}}
 
 
 def measure_e2e(pkg, L, wl, flags, steps, ws, dist):

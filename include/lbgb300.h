@@ -92,7 +92,10 @@ int lb_abi_release_d2q9(DataD2Q9 *data);
 int lb_abi_release_d3q19(DataD3Q19 *data);
 /* global conservation sums over non-solid nodes, accumulated in FP64 on the
  * GPU from the moment arrays: out = {mass, mom_x, mom_y, mom_z, kinetic
- * energy, max|u|, n_fluid}.  Blocks the calling thread until done. */
+ * energy, max|u|, n_fluid}.  Sums on the device current at the call, with
+ * scratch kept per device (allocated by the first call on that device), so
+ * the pointers in *data must be that device's.  Blocks the calling thread
+ * until done. */
 int lb_reduce_d2q9(const DataD2Q9 *data, double out[7]);
 int lb_reduce_d3q19(const DataD3Q19 *data, double out[7]);
 /* No counterpart in the reference.  The sums of lb_reduce_d3q19 for callers
@@ -103,9 +106,11 @@ int lb_reduce_d3q19(const DataD3Q19 *data, double out[7]);
  * loads the library keeps until the process exits.  Lattices of more than
  * 153 288 704 nodes are rejected with LB_ERR_ARG and a message in
  * lb_abi_last_error().  The first call on a device looks up the array's
- * device address (make it before any stream capture begins).  Calls share the
- * array, so calls that overlap on the GPU race; results equal
- * lb_reduce_d3q19's up to FP64 summation order. */
+ * device address.  Every call blocks the calling thread (it ends with a
+ * synchronous copy of the 7 results to *out), so it must not be called while
+ * a stream capture is in progress.  Calls share the array, so calls that
+ * overlap on the GPU race; results equal lb_reduce_d3q19's up to FP64
+ * summation order. */
 int lb_reduce_d3q19_noalloc(const DataD3Q19 *data, double out[7]);
 /* The reference's per-step host sequence (SimulationD3Q19::runLBM, reference
  * src/simulation_d3q19.cu:350-430, without the GL map/unmap and the extra

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/lbgb300.h"
@@ -1024,30 +1025,59 @@ int lb_vtk_save_ctx(lb_ctx *c, const char *dir, int vtk_id) {
 }
 
 // ----------------------------------------------------------------- drop-in reductions
+// Scratch (first-pass partials + the 7 results) of the drop-in reductions,
+// one allocation per device ordinal, made on the first call with that device
+// current: the caller may drive several devices (one DataD3Q19 per device,
+// as the reference's host loop does), and each call sums on the device that
+// is current when it is made.
 static std::mutex g_red_mu;
-static double *g_red = nullptr;  // partials + result, allocated on first use
+static std::unordered_map<int, double *> g_red;  // device ordinal -> scratch
 
-static int abi_reduce(const float *rho, const float *ux, const float *uy, const float *uz,
-                      const void *solid, long N, double out[7]) {
+static int abi_reduce(const char *where, const float *rho, const float *ux, const float *uy,
+                      const float *uz, const void *solid, long N, double out[7]) {
     std::lock_guard<std::mutex> l(g_red_mu);
-    if (!g_red && cudaMalloc(&g_red, sizeof(double) * (reduce_partials_size() + 8)) != cudaSuccess)
-        return LB_ERR_NOMEM;
-    double *res = g_red + reduce_partials_size();
-    cudaError_t e = launch_reduce(rho, ux, uy, uz, reinterpret_cast<const uint8_t *>(solid), 0xff,
-                                  N, g_red, res, 0);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        abi_record_error(where, cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    double *&scratch = g_red[dev];
+    if (!scratch) {
+        e = cudaMalloc(&scratch, sizeof(double) * (reduce_partials_size() + 8));
+        if (e != cudaSuccess) {
+            scratch = nullptr;
+            abi_record_error(where, cudaGetErrorString(e));
+            return LB_ERR_NOMEM;
+        }
+    }
+    double *res = scratch + reduce_partials_size();
+    e = launch_reduce(rho, ux, uy, uz, reinterpret_cast<const uint8_t *>(solid), 0xff, N,
+                      scratch, res, 0);
     if (e == cudaSuccess) e = cudaMemcpy(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost);
-    return e == cudaSuccess ? LB_OK : LB_ERR_CUDA;
+    if (e != cudaSuccess) {
+        abi_record_error(where, cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    return LB_OK;
 }
 
 int lb_reduce_d3q19(const DataD3Q19 *d, double out[7]) {
-    if (!d || !out) return LB_ERR_ARG;
-    return abi_reduce(d->rho, d->ux, d->uy, d->uz, d->solid,
+    if (!d || !out) {
+        abi_record_error("lb_reduce_d3q19", "null data or output");
+        return LB_ERR_ARG;
+    }
+    return abi_reduce("lb_reduce_d3q19", d->rho, d->ux, d->uy, d->uz, d->solid,
                       (long)d->width * d->height * d->depth, out);
 }
 
 int lb_reduce_d2q9(const DataD2Q9 *d, double out[7]) {
-    if (!d || !out) return LB_ERR_ARG;
-    return abi_reduce(d->rho, d->ux, d->uy, nullptr, d->solid, (long)d->width * d->height, out);
+    if (!d || !out) {
+        abi_record_error("lb_reduce_d2q9", "null data or output");
+        return LB_ERR_ARG;
+    }
+    return abi_reduce("lb_reduce_d2q9", d->rho, d->ux, d->uy, nullptr, d->solid,
+                      (long)d->width * d->height, out);
 }
 
 // ----------------------------------------------------------------- device helpers

@@ -14,8 +14,9 @@
 // array, not a device address: a kernel given it would fault or, where the GPU
 // can reach host memory, silently use the wrong memory.  The device address is
 // obtained once per device with cudaGetSymbolAddress, with that device current,
-// on the first call made on that device; make that first call before any
-// stream capture begins.
+// on the first call made on that device.  Every call blocks the calling thread:
+// it ends with a synchronous copy of the 7 results into the caller's host
+// array, so no call may be made while a stream capture is in progress.
 //
 // All calls share the one array and each call leaves its partials in it.
 // Nothing needs clearing between calls: every first-pass block overwrites its
@@ -34,6 +35,9 @@ constexpr int kScratchDoubles = 16384;                           // 128 KiB per 
 constexpr long kNodesPerBlock = 65536;                           // first-pass block covers 64 Ki nodes
 constexpr long kMaxBlocks = (kScratchDoubles - 8) / 7;           // 7 partials per block + 7 results
 constexpr long kMaxNodes = kMaxBlocks * kNodesPerBlock;          // 153 288 704 nodes
+// the largest lattice puts its 7 results in the array's last slots
+static_assert(7 * kMaxBlocks + 7 <= kScratchDoubles, "scratch holds every partial and result");
+static_assert(kMaxNodes == 153288704L, "the limit the error message and the header state");
 
 static __device__ __align__(256) double g_reduce_scratch[kScratchDoubles];
 

@@ -34,8 +34,9 @@
 //
 // Every mbarrier wait is bounded (wait_limit polls of about a microsecond for
 // a stage; ST_WAIT in the library's launches); a block that gives up raises
-// the device error word, waits (bounded by ST_WAIT) for the copies it still
-// has in flight and returns.  sc_stage_wait_selftest makes the first wait run
+// the device error word, waits (bounded by ST_WAIT) for the stages it still
+// has in flight, drains its threads' own copies (cp.async.wait_all) and
+// returns.  sc_stage_wait_selftest makes the first wait run
 // out (wait_limit 0) to exercise that path.  (A first form copied each stage row with one cp.async.bulk per
 // population and row, 228 copies per stage: 20.9 GLUPS for FP32 and 16-bit
 // alike at 256^3, bound by the number of copies, not their bytes.)
@@ -257,6 +258,11 @@ __global__ void __launch_bounds__(ST_THREADS, StageShape<S>::MIN_BLOCKS)
             if (tid == 0 && a.err) atomicExch(a.err, 1);
             for (int i = j; i < j + SS::SLOTS && i < nst; i++)
                 mbar_wait(&full[i % SS::SLOTS], (uint32_t)((i / SS::SLOTS) & 1), ST_WAIT);
+            // then drain this thread's own copies whatever those waits saw, so
+            // that none can land in shared memory that the next block resident
+            // on this SM reuses (memory copies always complete; no other party
+            // has to act for this wait to end)
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
             return false;
         }
         if (j + SS::SLOTS < nst) cp.issue(a, stage + slot * SS::ELEMS, &full[slot], zs + SS::SLOTS);

@@ -16,7 +16,26 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "liblboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "liblbref.so")
-REF_SRC = "/root/reference/src"
+
+
+def ref_dir():
+    """Location of the reference tree: the environment variable
+    LATTIBOL_REF_DIR, else the default of the build recipe (oracle/Makefile,
+    ``make ref-dir``).  Callers check that it exists: it does not where only
+    this repository was copied."""
+    d = os.environ.get("LATTIBOL_REF_DIR")
+    if d:
+        return d
+    try:
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref-dir"], capture_output=True, text=True,
+                           check=True)
+        return r.stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
+
+def ref_src():
+    return os.path.join(ref_dir(), "src")
 
 PSI_REF = 0
 PSI_EXP1 = 1
@@ -40,7 +59,7 @@ def build(ref=None):
     reference's own kernels for the host into oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref is None:
-        ref = os.path.isdir(REF_SRC)
+        ref = os.path.isdir(ref_src())
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
@@ -61,7 +80,7 @@ def ref_lib():
     """The reference's kernels compiled for the host, or None where the
     reference sources are absent."""
     if not os.path.exists(REF_PATH):
-        if not os.path.isdir(REF_SRC):
+        if not os.path.isdir(ref_src()):
             return None
         build(ref=True)
     return ctypes.CDLL(REF_PATH)

@@ -4,6 +4,7 @@ case), read by the case-file oracle (oracle/case_oracle.py).
 
 Run from the repository root where the reference tree exists:
     python tests/golden/make_case_fixtures.py [reference root]
+(default: LATTIBOL_REF_DIR, else the oracle recipe's default location)
 
 cases.json holds, per case, the parsed parameters (floats as IEEE-754 bit
 patterns) and, for 2-D cases, the mask's size, solid count and SHA-256; for
@@ -79,4 +80,5 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import lb_oracle
+    main(sys.argv[1] if len(sys.argv) > 1 else lb_oracle.ref_dir())

@@ -12,10 +12,13 @@ import numpy as np
 import pytest
 
 import case_oracle as co
+import lb_oracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-SAMPLES = "/root/reference/samples"  # present only where the reference tree is
+# the reference's sample cases: present only where the reference tree is (its
+# location: LATTIBOL_REF_DIR, else the oracle recipe's default)
+SAMPLES = os.path.join(lb_oracle.ref_dir() or "/nonexistent", "samples")
 
 
 def lib(pkg):
