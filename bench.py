@@ -151,6 +151,7 @@ def run_ensemble(args, dist, ws, rank, local):
     GLUPS counts the nodes of all domains."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
+    select_device(pkg, ws, local)
     nx, ny, G, rho = pkg.droplet_ensemble(args.domains or ENSEMBLE["domains"],
                                           seed=ENSEMBLE["seed"])
     steps = args.steps if args.steps else ENSEMBLE["steps"]
@@ -207,86 +208,71 @@ def run_ensemble(args, dist, ws, rank, local):
     return 0
 
 
-CLOSURE = {"U0": 0.05, "Re": 1600.0, "fine": 512, "factor": 4, "t_end": 10.0,
-           "ke_every_coarse": 64, "train_snapshots": 16, "train_steps": 3000,
-           "batch": 16384, "lr": 2e-3}
+CLOSURE = {"U0": 0.05, "Re": 1600.0, "fine": 512, "factors": (2, 4, 8, 16), "plain_only": (2,),
+           "t_end": 10.0, "fine_every": 256, "train_snapshots": 16, "train_steps": 3000,
+           "batch": 16384, "lr": 2e-3, "avg_radius": 1, "max_ke_error": 0.01}
 
 
 def run_closure(args, dist, ws, rank, local):
     """Learned closure for the under-resolved Taylor-Green vortex (Re 1600,
-    U0 = 0.05): fine 512^3 FP32 BGK run, Favre box filter by 4 onto 128^3
-    (training data at 16 snapshots, filtered kinetic energy every 64 coarse
-    steps), GPU training of the closure network, then 128^3 coarse runs with
-    plain BGK (the fallback) and with the closure over 10 convective times.
-    value = wall time of the fine run / wall time of the closure run, with the
-    kinetic-energy decay error of both coarse runs against the filtered fine
-    run."""
+    U0 = 0.05) over coarse grids 256^3 .. 32^3.  One fine 512^3 FP32 BGK run
+    is Favre box-filtered onto every coarse grid (the reference kinetic
+    energy every 256 fine steps; training data at 16 snapshots); a closure
+    network is trained on the GPU for each of 128^3, 64^3 and 32^3 and its
+    output scale calibrated on the first half of the trajectory; plain BGK
+    runs on every grid.  value = the closure's speed-up over the plain FP32
+    path at equal kinetic-energy error: the wall time of the cheapest plain
+    run whose KE-decay error is at most the closure run's, divided by the
+    closure run's -- the best such pair among the closure runs with a KE
+    error of at most 1 % (every pair is listed)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
+    select_device(pkg, ws, local)
     C = pkg.closure
     cfg = dict(CLOSURE)
-    if args.size:
-        cfg["fine"] = args.size[0]
-    nf, fac, U0, Re = cfg["fine"], cfg["factor"], cfg["U0"], cfg["Re"]
-    nc = nf // fac
-    steps_c = int(round(cfg["t_end"] * (nc / (2 * np.pi)) / U0))
-    every = cfg["ke_every_coarse"]
-    nsamp = steps_c // every
-    train_at = set(np.linspace(0, nsamp, cfg["train_snapshots"]).astype(int).tolist())
-    fr = C.FineRun(nf, fac, U0, Re)
-    feat = C.DeviceArray(len(train_at) * nc ** 3 * 19)
-    targ = C.DeviceArray(len(train_at) * nc ** 3)
-    slot = 0
-    ke_ref = []
-    for i in range(nsamp + 1):
-        if i:
-            fr.advance(every * fac)
-        if i in train_at:
-            ke_ref.append(fr.sample(feat, targ, slot * nc ** 3))
-            slot += 1
-        else:
-            ke_ref.append(fr.sample())
-    fine_seconds, fine_steps = fr.seconds, fr.steps
-    fr.close()
-    net = C.Mlp(seed=2)
-    t0 = time.perf_counter()
-    log = net.train_device(feat, targ, slot * nc ** 3, steps=cfg["train_steps"],
-                           batch=cfg["batch"], lr=cfg["lr"])
-    train_seconds = time.perf_counter() - t0
-    feat.free()
-    targ.free()
-    ke_plain, plain_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every,
-                                           tuning=args.tuning)
+    nf = args.size[0] if args.size else cfg["fine"]
+    factors = tuple(f for f in cfg["factors"] if nf // f >= 8)
     with ClockSampler(local) as clk:
-        ke_learn, learn_seconds = C.coarse_run(nc, U0, Re, nsamp * every, every, mlp=net,
-                                               tuning=args.tuning)
-    net.close()
-    e_plain, e_learn = C.ke_error(ke_plain, ke_ref), C.ke_error(ke_learn, ke_ref)
+        sw = C.resolution_sweep(nf, factors, U0=cfg["U0"], Re=cfg["Re"], t_end=cfg["t_end"],
+                                fine_every=cfg["fine_every"],
+                                train_snapshots=cfg["train_snapshots"],
+                                train_steps=cfg["train_steps"], batch=cfg["batch"], lr=cfg["lr"],
+                                avg_radius=cfg["avg_radius"], plain_only=cfg["plain_only"])
     if rank != 0:
         return 0
-    plain_blowup = None
-    if not np.all(np.isfinite(ke_plain)):
-        plain_blowup = int(np.argmax(~np.isfinite(ke_plain)) * every)
-    line = {"metric": "closure_speedup_at_ke_error", "value": fine_seconds / learn_seconds,
-            "unit": "x", "n_gpus": ws, "steps": nsamp * every, "warmup": 0,
-            "ms_per_step": 1e3 * learn_seconds / (nsamp * every), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
-            "config": {"workload": "closure_tgv_re1600_%d_to_%d" % (nf, nc), "U0": U0, "Re": Re,
-                       "fine_nodes": nf ** 3, "coarse_nodes": nc ** 3, "filter": "Favre box %d^3"
-                       % fac, "convective_times": cfg["t_end"],
-                       "mlp": "19-64-64-1 ReLU, BF16 tensor cores, FP32 accumulate",
-                       "training": {"snapshots": slot, "samples": slot * nc ** 3,
+    pairs = C.speedup_at_equal_error(sw["runs"])
+    best = C.headline(pairs, max_error=cfg["max_ke_error"])
+    closure_runs = [r for r in sw["runs"] if r["kind"] == "closure"]
+    c128 = next((r for r in closure_runs if r["n"] == nf // 4), None)
+    best_run = next((r for r in closure_runs if best and r["n"] == best["closure_n"]), None)
+    line = {"metric": "closure_speedup_at_equal_ke_error",
+            "value": best["speedup"] if best else None, "unit": "x", "n_gpus": ws,
+            "steps": best_run["steps"] if best_run else None, "warmup": 0,
+            "ms_per_step": 1e3 * best_run["seconds"] / best_run["steps"] if best_run else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+bf16", "data": "synthetic",
+            "config": {"workload": "closure_tgv_re1600_fine%d" % nf, "U0": cfg["U0"],
+                       "Re": cfg["Re"], "fine_nodes": nf ** 3,
+                       "coarse_grids": [nf // f for f in factors],
+                       "filter": "Favre box, factor = fine / coarse",
+                       "convective_times": cfg["t_end"],
+                       "mlp": "19-64-64-1 ReLU, BF16 tensor cores (tcgen05), FP32 accumulate",
+                       "training": {"snapshots": cfg["train_snapshots"],
                                     "adam_steps": cfg["train_steps"], "batch": cfg["batch"],
-                                    "final_loss": float(np.mean(log[-20:]))}},
-            "closure": {"ke_error_learned": e_learn, "ke_error_plain": e_plain,
-                        "plain_blowup_step": plain_blowup, "fine_seconds": fine_seconds,
-                        "fine_steps": fine_steps, "coarse_closure_seconds": learn_seconds,
-                        "coarse_plain_seconds": plain_seconds, "train_seconds": train_seconds,
-                        "coarse_closure_glups": nc ** 3 * nsamp * every / learn_seconds / 1e9,
-                        "fine_glups": nf ** 3 * fine_steps / fine_seconds / 1e9,
-                        "ke_curve_stride_coarse_steps": every,
-                        "ke_ref": [round(v / ke_ref[0], 5) for v in ke_ref[::4]],
-                        "ke_learned": [round(float(v / ke_learn[0]), 5) for v in ke_learn[::4]]},
+                                    "target": "nu_t of the filtered sub-grid stress, both "
+                                              "contractions averaged over 3^3 coarse cells",
+                                    "inputs": "inputs never excited in the training data "
+                                              "get zero first-layer weights",
+                                    "output_scale": "fitted on the first half of the "
+                                                    "trajectory from %s"
+                                                    % list(C.CALIBRATION_SCALES)},
+                       "ke_error": "RMS over the samples of E/E0 against the filtered fine run",
+                       "headline": "best speed-up among closure runs with KE error <= %g"
+                                   % cfg["max_ke_error"]},
+            "closure": {"equal_error_pairs": pairs, "best": best, "runs": sw["runs"],
+                        "fine_seconds": sw["fine_seconds"], "fine_steps": sw["fine_steps"],
+                        "closure_128_vs_fine_run": (sw["fine_seconds"] / c128["seconds"])
+                                                   if c128 else None},
             "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
@@ -365,6 +351,13 @@ def dist_init(ws, backend):
     import torch.distributed as dist
     dist.init_process_group(backend)
     return dist
+
+
+def select_device(pkg, ws, local):
+    """One process per GPU: this rank's library calls go to GPU `local`."""
+    if ws > 1:
+        rc = pkg.lib().lb_set_device(local)
+        assert rc == 0, "lb_set_device(%d) failed" % local
 
 
 def dist_max(dist, v):
@@ -451,6 +444,12 @@ def main():
     ap.add_argument("--workload", default="channel",
                     choices=sorted(WORKLOADS) + ["ensemble", "closure"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--parallelism", default="auto", choices=["auto", "replicas", "zslab"],
+                    help="channel with N > 1 ranks: one z-slab of one lattice per rank (auto, "
+                         "zslab) or independent replicas")
+    ap.add_argument("--slabs", type=int, default=0,
+                    help="channel, one rank: cut the lattice into this many z-slabs stepped "
+                         "as one group on the GPU")
     ap.add_argument("--no-f16", action="store_true",
                     help="channel: skip the 16-bit storage figure beside the FP32 one")
     ap.add_argument("--e2e-steps", type=int, default=2000)
@@ -484,9 +483,13 @@ def main():
     args.warmup = max(args.warmup, 3)
 
     ws, rank, local = dist_env()
+    if wl.name.startswith("channel") and (args.parallelism == "zslab" or args.slabs > 1 or
+                                          (args.parallelism == "auto" and ws > 1)):
+        return run_zslab(args, wl, ws, rank, local)
     dist = dist_init(ws, "gloo")
     import __graft_entry__ as ge
     pkg = ge.load_package()
+    select_device(pkg, ws, local)
     L = pkg.lib()
     N = wl.N
     nx, ny, nz = wl.size
@@ -550,6 +553,107 @@ def main():
     if not args.no_cpu_baseline and ws == 1:
         cb = cpu_baseline(wl, budget_s=float(os.environ.get("LB_CPU_BUDGET_S", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line))
+    return 0
+
+
+def channel_flags(nx, ny, nz, spheres):
+    """y/z walls and one sphere of radius 16 at (64, 64, 64 + 128 s) for each
+    s < spheres (the channel of every 128 planes)."""
+    fl = np.zeros((nz, ny, nx), np.uint8)
+    fl[:, 0, :] = fl[:, -1, :] = 1
+    fl[0, :, :] = fl[-1, :, :] = 1
+    z, y, x = np.ogrid[0:nz, 0:ny, 0:nx]
+    for sp in range(spheres):
+        fl[(x - 64) ** 2 + (y - 64) ** 2 + (z - 64 - 128 * sp) ** 2 <= 16 * 16] = 1
+    return fl.reshape(-1)
+
+
+def run_zslab(args, wl, ws, rank, local):
+    """The channel cut into z-slabs (include/lbgb300.h part 7).  One rank:
+    the 256x128x128 lattice in --slabs slabs stepped as one group on the GPU
+    (faces moved by device copies, the interior planes of each slab on a
+    second stream).  N ranks (one per GPU): a 256x128x(128 N) channel with a
+    sphere in every 128 planes, rank r holding planes 128 r .. 128 r + 127
+    and exchanging its two faces with its z-neighbours over NCCL every step
+    (weak scaling: 128 planes per GPU)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    S = pkg.slab
+    nx, ny, nz1 = wl.size
+    nzg = nz1 * ws
+    flags = channel_flags(nx, ny, nzg, max(1, nzg // 128))
+    P = nx * ny
+    kw = dict(tau_inv=np.float32(1 / wl.tau), force=tuple(np.float32(v) for v in wl.force),
+              storage=wl.storage, rho_ref=wl.rho_ref)
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        select_device(pkg, ws, local)
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        bounds = [(rank * nz1, nz1)]
+    else:
+        bounds = S.slab_bounds(nzg, max(1, args.slabs))
+    slabs = []
+    for z0, nz in bounds:
+        sl = S.Slab(nx, ny, nzg, z0, nz, **kw)
+        sl.set_flags(np.ascontiguousarray(flags.reshape(nzg, P)[sl.planes()].reshape(-1)))
+        sl.init_equilibrium(None)
+        slabs.append(sl)
+    n0 = sum(sl.launches() for sl in slabs)
+    if ws > 1:
+        import torch
+        sr = S.SlabRank(slabs[0], S.SlabExchange(dist, rank, ws))
+        sr.step(max(args.warmup, 3))
+        slabs[0].synchronize()
+        dist.barrier()
+        n0 = slabs[0].launches()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            t0.record(sr.stream)
+            sr.step(args.steps)
+            t1.record(sr.stream)
+            t1.synchronize()
+        ms = t0.elapsed_time(t1)
+        ms = dist_max(dist, ms)
+    else:
+        grp = S.SlabGroup(slabs)
+        grp.step(max(args.warmup, 3))
+        grp.synchronize()
+        n0 = grp.launches()
+        with ClockSampler(local) as clk:
+            ms = grp.time_steps(args.steps)
+    launches = sum(sl.launches() for sl in slabs) - n0
+    mom = slabs[0].moments()
+    assert np.isfinite(slabs[0].own(mom[0])).all()
+    face_bytes = slabs[0].face_bytes
+    for sl in slabs:
+        sl.close()
+    if rank != 0:
+        return 0
+    N = nx * ny * nzg
+    peak, peak_kind = measured_peak()
+    achieved = wl.bytes_per_lu * N / ws / (ms / args.steps * 1e-3) / 1e9
+    cfg = wl.config(ws)
+    cfg.update({"workload": "%s_zslab_%dx%dx%d" % (wl.name, nx, ny, nzg),
+                "nodes": [nx, ny, nzg], "parallelism": "zslab",
+                "slabs": len(bounds) if ws == 1 else ws,
+                "slab_planes": [nz for _, nz in bounds] if ws == 1 else nz1,
+                "exchange": "device copies between the slabs of one GPU" if ws == 1 else
+                            "NCCL send/recv of the two faces with the z-neighbours",
+                "exchange_bytes_per_slab_step": 2 * face_bytes,
+                "spheres": "radius 16 at (64, 64, 64 + 128 s)"})
+    line = {"metric": "GLUPS", "value": N * args.steps / (ms * 1e-3) / 1e9, "unit": "GLUPS",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic", "config": cfg,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "bytes_per_lu": wl.bytes_per_lu, "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
 

@@ -340,6 +340,13 @@ int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, floa
  * filtered field */
 int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
                       float *features_dev, float *targets_dev, double *ke_mean);
+/* the same with the target's two contractions T_dev : S and S : S summed over
+ * the (2 avg_radius + 1)^3 coarse cells around each cell (periodic) before
+ * nu_t = max(0, -sum(T_dev : S) / (2 sum(S : S))) is formed (avg_radius 0 is
+ * lb_closure_sample) */
+int lb_closure_sample_avg(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
+                          int avg_radius, float *features_dev, float *targets_dev,
+                          double *ke_mean);
 /* device pointers of a context's moment fields (valid until lb_destroy) and
  * its extents */
 int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **uz);
@@ -465,8 +472,63 @@ int lb_checkpoint_info(const char *path, lb_config *cfg, int64_t *steps);
  * lb_checkpoint_load) */
 int64_t lb_steps_done(const lb_ctx *ctx);
 
+/* ======================================================================== */
+/* Part 7: z-slab decomposition (several devices or processes, one lattice) */
+/* ======================================================================== */
+/* Replaces the reference's x-slab halo exchange between devices:
+ * get_border_d3q19 (src/get_border.cu:59-98) packs a face, copy_border_devices
+ * (src/copy_border.cu:49-81) moves it to the neighbour, apply_border_d3q19
+ * (src/apply_border.cu:58-97) unpacks it, driven once per step from
+ * src/simulation_d3q19.cu:363-406.  Here the lattice is cut along z, the
+ * slowest axis, so each of the 5 populations that cross a face is one
+ * contiguous plane: lb_slab_step packs them (get_border), the caller or
+ * lb_slab_group_step moves them (copy_border) and lb_slab_unpack writes them
+ * into the receiving slab's ghost plane (apply_border).  The planes of the
+ * step that the exchange does not need run on a second stream meanwhile.
+ *
+ * A slab context holds global planes z0 .. z0 + nz - 1 of a D3Q19 native-mode
+ * lattice without Shan-Chen (global config *global, periodic in z) plus one
+ * ghost plane below and one above, so every per-node array it takes or gives
+ * (lb_set_flags, lb_set_populations, lb_get_populations, lb_init_equilibrium,
+ * lb_get_moments) covers nz + 2 planes: global planes z0 - 1 .. z0 + nz, z
+ * wrapped.  Flags must be given for the ghost planes too.  Moments of the
+ * ghost planes are not computed; lb_reduce sums the own planes.  lb_step,
+ * lb_run_probe, checkpoints and the closure are not available on a slab.
+ *
+ * Step protocol, per time step, with the face buffers on the slab's device
+ * (face_bytes each = 5 nx ny stored values, [5][nx*ny], populations 6, 10, 14,
+ * 16, 18 for the lower face and 5, 9, 13, 15, 17 for the upper one):
+ *   lb_slab_step(ctx, moments, to_below, to_above);   - queues the step and
+ *        the new faces on lb_stream(ctx)
+ *   (transport on lb_stream(ctx): to_below -> the lower neighbour's from_above,
+ *    to_above -> the upper neighbour's from_below)
+ *   lb_slab_unpack(ctx, from_below, from_above);     - ghost planes of the new state
+ * Before the first step the ghost planes hold what lb_set_populations or
+ * lb_init_equilibrium gave them; lb_slab_pack gives the current faces (to
+ * refresh the ghosts of a state set some other way).  Results are bit-identical
+ * to the same steps of one context over the whole lattice. */
+int lb_slab_create(const lb_config *global, int z0, int nz, lb_ctx **out);
+int lb_slab_info(const lb_ctx *ctx, int *z0, int *nz, int *nz_global, size_t *face_bytes);
+/* the context's CUDA stream (cudaStream_t) for an external transport */
+void *lb_stream(lb_ctx *ctx);
+int lb_slab_pack(lb_ctx *ctx, void *to_below, void *to_above);
+int lb_slab_step(lb_ctx *ctx, int moments, void *to_below, void *to_above);
+int lb_slab_unpack(lb_ctx *ctx, const void *from_below, const void *from_above);
+/* nsteps steps of all n slabs of one lattice held by this process on the
+ * current device (slabs[i] the z-neighbour above slabs[i-1], periodic), the
+ * faces moved by device copies; the last step writes the moments.
+ * Asynchronous (lb_synchronize each slab). */
+int lb_slab_group_step(lb_ctx *const *slabs, int n, int nsteps);
+/* lb_slab_group_step timed on the device: *ms from an event before any slab's
+ * first launch to one after every slab's last (blocks until done) */
+int lb_slab_group_time(lb_ctx *const *slabs, int n, int nsteps, float *ms);
+
 /* ---- device helpers (tests and hosts without their own allocator) ------ */
 int lb_device_count(int *n);
+/* the device this thread's later calls (lb_create, lb_slab_create, ...) use;
+ * one process per GPU selects its own (its local rank) before creating any
+ * context */
+int lb_set_device(int dev);
 int lb_malloc(void **ptr, size_t bytes);
 int lb_free(void *ptr);
 int lb_malloc_host(void **ptr, size_t bytes); /* page-locked host memory */

@@ -20,5 +20,6 @@ def lib():
 from .lattice import (DeviceData, Ensemble, Lattice, LBError, W2, W3,  # noqa: E402,F401
                       droplet_ensemble)
 from . import closure  # noqa: E402,F401
+from . import slab  # noqa: E402,F401
 from . import case  # noqa: E402,F401
 from .case import Input, Output, SimulationD2Q9, SimulationD3Q19  # noqa: E402,F401

@@ -182,6 +182,9 @@ PROTOTYPES = [
                                      _c.c_float, _c.c_void_p]),
     ("lb_closure_sample", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_float, _c.c_float, _c.c_float,
                                      _c.c_void_p, _c.c_void_p, _c.POINTER(_c.c_double)]),
+    ("lb_closure_sample_avg", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_float, _c.c_float,
+                                         _c.c_float, _c.c_int, _c.c_void_p, _c.c_void_p,
+                                         _c.POINTER(_c.c_double)]),
     ("lb_device_fields", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_void_p)] * 4),
     ("lb_extents", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3),
     ("lb_tcgen05_selftest", _c.c_int, [_c.c_void_p, _c.POINTER(_c.c_int)]),
@@ -207,7 +210,19 @@ PROTOTYPES = [
     ("lb_checkpoint_info", _c.c_int, [_c.c_char_p, _c.POINTER(lb_config),
                                       _c.POINTER(_c.c_int64)]),
     ("lb_steps_done", _c.c_int64, [_c.c_void_p]),
+    ("lb_slab_create", _c.c_int, [_c.POINTER(lb_config), _c.c_int, _c.c_int,
+                                  _c.POINTER(_c.c_void_p)]),
+    ("lb_slab_info", _c.c_int, [_c.c_void_p] + [_c.POINTER(_c.c_int)] * 3
+     + [_c.POINTER(_c.c_size_t)]),
+    ("lb_stream", _c.c_void_p, [_c.c_void_p]),
+    ("lb_slab_pack", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p]),
+    ("lb_slab_step", _c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p, _c.c_void_p]),
+    ("lb_slab_unpack", _c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p]),
+    ("lb_slab_group_step", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_int, _c.c_int]),
+    ("lb_slab_group_time", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_int, _c.c_int,
+                                      _c.POINTER(_c.c_float)]),
     ("lb_device_count", _c.c_int, [_c.POINTER(_c.c_int)]),
+    ("lb_set_device", _c.c_int, [_c.c_int]),
     ("lb_malloc", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),
     ("lb_free", _c.c_int, [_c.c_void_p]),
     ("lb_malloc_host", _c.c_int, [_c.POINTER(_c.c_void_p), _c.c_size_t]),

@@ -168,15 +168,21 @@ class FineRun:
             self.seconds += time.perf_counter() - t0
             self.steps += fine_steps
 
-    def sample(self, feat=None, targ=None, offset=0):
+    def sample(self, feat=None, targ=None, offset=0, factor=None, avg_radius=0):
         """Filtered resolved KE (mean per coarse cell); with device arrays,
-        writes features/targets of all coarse cells starting at row offset."""
+        writes features/targets of all coarse cells starting at row offset.
+        factor: another filter width than the run's own (coarse grid
+        n_fine / factor); avg_radius: the target's neighbourhood averaging
+        (lb_closure_sample_avg)."""
+        fac = self.fac if factor is None else int(factor)
+        nc = self.nf // fac
         ke = ctypes.c_double()
         f = feat.offset(offset * 19) if feat is not None else None
         t = targ.offset(offset) if targ is not None else None
-        rc = _lib().lb_closure_sample(self.lat.h, self.fac, np.float32(self.nu_c),
-                                      np.float32(self.s_ref), np.float32(self.z_max), f, t,
-                                      ctypes.byref(ke))
+        rc = _lib().lb_closure_sample_avg(self.lat.h, fac, np.float32(viscosity(nc, self.U0, self.Re)),
+                                          np.float32(self.U0 * 2 * np.pi / nc),
+                                          np.float32(self.z_max), int(avg_radius), f, t,
+                                          ctypes.byref(ke))
         if rc != abi.LB_OK:
             raise LBError("lb_closure_sample: %d" % rc)
         return ke.value
@@ -227,3 +233,160 @@ def ke_error(coarse, reference):
     if not np.all(np.isfinite(a)):
         return float("inf")
     return float(np.sqrt(np.mean((a - b) ** 2)))
+
+
+def active_inputs(feat, n_rows, rows_per_snapshot, probe=20000):
+    """Which of the 19 inputs are non-zero somewhere in the training rows
+    (a probe of every snapshot's first rows).  The stress features and |S|
+    are; the higher non-equilibrium moments are zero in filtered fine data
+    (they vanish at first order), so their first-layer weights would get no
+    gradient and keep their random initial values."""
+    active = np.zeros(Mlp.N_IN, bool)
+    for off in range(0, n_rows, rows_per_snapshot):
+        m = min(rows_per_snapshot, probe, n_rows - off)
+        rows = feat.download((off + m) * Mlp.N_IN).reshape(-1, Mlp.N_IN)[off:off + m]
+        active |= np.abs(rows).max(axis=0) > 0
+    return active
+
+
+def zero_inputs(net, active):
+    """First-layer weights of the inactive inputs set to zero (they then get
+    zero gradients and stay zero: the network ignores inputs it never saw)."""
+    p = net.params()
+    p[:64 * Mlp.N_IN].reshape(64, Mlp.N_IN)[:, ~np.asarray(active)] = 0
+    net.set_params(p)
+
+
+def scale_output(net, c, base=None):
+    """The network's output scaled by c (output layer w3, b3; the eddy
+    viscosity nu0 * clamp(y, 0, z_max) then scales with it)."""
+    p = (net.params() if base is None else base).copy()
+    p[-65:] *= np.float32(c)
+    net.set_params(p)
+
+
+CALIBRATION_SCALES = (1.0, 0.7, 0.5, 0.35, 0.25, 0.18, 0.12)
+
+
+def calibrate(net, nc, U0, Re, ke_ref, every, steps, scales=CALIBRATION_SCALES, window=0.5):
+    """A posteriori fit of one scalar: the output scale c (from `scales`) whose
+    coarse run best tracks the reference kinetic energy over the first
+    `window` of the trajectory.  The coarse LBM dissipates by itself (its
+    truncation error acts as an implicit sub-grid model), so the sub-grid
+    dissipation fitted a priori from the filtered stress is too much for it;
+    c takes out that double count.  The remaining part of the trajectory is
+    not seen by the fit.  Returns (c, {c: window error})."""
+    base = net.params()
+    nwin = max(1, int(round(len(ke_ref) * window)) - 1)
+    errs = {}
+    for c in scales:
+        scale_output(net, c, base)
+        ke, _ = coarse_run(nc, U0, Re, nwin * every, every, mlp=net)
+        errs[c] = ke_error(ke, ke_ref[:nwin + 1])
+    best = min(errs, key=lambda c: errs[c])
+    scale_output(net, best, base)
+    return best, errs
+
+
+def resolution_sweep(n_fine, factors, U0=0.05, Re=1600.0, t_end=10.0, fine_every=256,
+                     train_snapshots=16, train_steps=3000, batch=16384, lr=2e-3, avg_radius=1,
+                     plain_only=(), seed=2, log=None):
+    """Plain coarse BGK against the learned closure over several coarse grids.
+
+    One fine run (n_fine^3) is box-filtered by every factor at every sample
+    (each fine_every fine steps): the reference kinetic energy of each coarse
+    grid and, at train_snapshots samples, its training data (features and
+    neighbourhood-averaged targets).  For each factor not in plain_only a
+    network is trained on that grid's data (inputs never excited in the data
+    masked), its output scale calibrated on the first half of the
+    trajectory, and run over the whole trajectory; every factor also gets a
+    plain BGK run.  Returns a dict with the fine run's time and one entry per
+    run (grid, kind, KE error, wall time of the steps, steps)."""
+    fr = FineRun(n_fine, factors[0], U0, Re)
+    steps_f = int(round(t_end * (n_fine / (2 * np.pi)) / U0))
+    nsamp = steps_f // fine_every
+    train_at = set(np.linspace(0, nsamp, train_snapshots).astype(int).tolist())
+    learned = [f for f in factors if f not in plain_only]
+    data = {}
+    for f in learned:
+        nc3 = (n_fine // f) ** 3
+        data[f] = (DeviceArray(len(train_at) * nc3 * 19), DeviceArray(len(train_at) * nc3))
+    ke = {f: [] for f in factors}
+    slot = 0
+    for i in range(nsamp + 1):
+        if i:
+            fr.advance(fine_every)
+        for f in factors:
+            if f in data and i in train_at:
+                nc3 = (n_fine // f) ** 3
+                ke[f].append(fr.sample(data[f][0], data[f][1], slot * nc3, factor=f,
+                                       avg_radius=avg_radius))
+            else:
+                ke[f].append(fr.sample(factor=f))
+        if i in train_at:
+            slot += 1
+    out = {"fine_seconds": fr.seconds, "fine_steps": fr.steps, "fine_n": n_fine, "runs": [],
+           "samples": nsamp + 1}
+    fr.close()
+    for f in factors:
+        nc = n_fine // f
+        every = fine_every // f
+        ke_p, t_p = coarse_run(nc, U0, Re, nsamp * every, every)
+        e_p = ke_error(ke_p, ke[f])
+        out["runs"].append({"n": nc, "kind": "plain", "ke_error": e_p, "seconds": t_p,
+                            "steps": nsamp * every})
+        if log:
+            log("plain %d^3: KE error %.5g, %.4f s" % (nc, e_p, t_p))
+        if f not in data:
+            continue
+        feat, targ = data.pop(f)
+        nc3 = nc ** 3
+        net = Mlp(seed=seed)
+        active = active_inputs(feat, slot * nc3, nc3)
+        zero_inputs(net, active)
+        t0 = time.perf_counter()
+        tlog = net.train_device(feat, targ, slot * nc3, steps=train_steps, batch=batch, lr=lr)
+        train_s = time.perf_counter() - t0
+        feat.free()
+        targ.free()
+        c, cal = calibrate(net, nc, U0, Re, ke[f], every, nsamp * every)
+        ke_l, t_l = coarse_run(nc, U0, Re, nsamp * every, every, mlp=net)
+        e_l = ke_error(ke_l, ke[f])
+        net.close()
+        out["runs"].append({"n": nc, "kind": "closure", "ke_error": e_l, "seconds": t_l,
+                            "steps": nsamp * every, "train_seconds": train_s,
+                            "final_loss": float(np.mean(tlog[-20:])), "output_scale": c,
+                            "calibration_errors": {str(k): v for k, v in cal.items()},
+                            "active_inputs": np.nonzero(active)[0].tolist(),
+                            "ke_curve": [round(float(v / ke_l[0]), 5) for v in ke_l[::4]]})
+        if log:
+            log("closure %d^3: KE error %.5g, %.4f s (scale %g)" % (nc, e_l, t_l, c))
+    out["ke_ref"] = {str(n_fine // f): [round(v / ke[f][0], 5) for v in ke[f][::4]]
+                     for f in factors}
+    return out
+
+
+def headline(pairs, max_error=0.01):
+    """The largest speed-up among the closure runs whose KE error is at most
+    max_error (None if there is none)."""
+    ok = [p for p in pairs if p["speedup"] and p["closure_ke_error"] <= max_error]
+    return max(ok, key=lambda p: p["speedup"], default=None)
+
+
+def speedup_at_equal_error(runs):
+    """For every closure run: the cheapest plain run whose KE error is at most
+    the closure's (finite), and the ratio of their wall times."""
+    plain = sorted([r for r in runs if r["kind"] == "plain" and np.isfinite(r["ke_error"])],
+                   key=lambda r: r["seconds"])
+    res = []
+    for r in runs:
+        if r["kind"] != "closure" or not np.isfinite(r["ke_error"]):
+            continue
+        match = next((p for p in plain if p["ke_error"] <= r["ke_error"]), None)
+        res.append({"closure_n": r["n"], "closure_ke_error": r["ke_error"],
+                    "closure_seconds": r["seconds"],
+                    "plain_n": match["n"] if match else None,
+                    "plain_ke_error": match["ke_error"] if match else None,
+                    "plain_seconds": match["seconds"] if match else None,
+                    "speedup": match["seconds"] / r["seconds"] if match else None})
+    return res

@@ -220,10 +220,11 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
     uint32_t phase = 0;
     bool ok = true;
 
-    // row-blocks r = bx + nbx (y + H z); 32-bit: a lattice has fewer than
-    // 2^31 of them (the node count itself is below 2^31)
-    const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
-    const int nrows = nbx * a.H * a.D;
+    // runs of 128 consecutive nodes r * 128 .. r * 128 + 127 (row after row, so
+    // a lattice narrower than 128 nodes still fills every row of the MMA tile);
+    // 32-bit: the node count is below 2^31
+    const int WH = a.W * a.H, ncell = WH * a.D;
+    const int nrows = (ncell + D3_BLOCK - 1) / D3_BLOCK;
     // a run of 128 cells: this thread's cell, its flags and pulled populations
     struct Run {
         int o;
@@ -232,11 +233,11 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
     };
     auto load = [&](int r, Run &u) {
         const int rr = a.reverse ? nrows - 1 - r : r;
-        const int bx = rr % nbx, yz = rr / nbx;
-        const int y = yz % a.H, z = yz / a.H;
-        const int x = bx * D3_BLOCK + t;
-        u.inside = x < a.W;
-        u.o = u.inside ? x + a.W * (y + a.H * z) : 0;
+        const int oo = rr * D3_BLOCK + t;
+        u.inside = oo < ncell;
+        u.o = u.inside ? oo : 0;
+        const int z = u.o / WH, rem = u.o - z * WH;
+        const int y = rem / a.W, x = rem - y * a.W;
         const uint8_t fl = u.inside ? a.flags[u.o] : CELL_WALL;
         u.fluid = !(fl & CELL_WALL);
         if (u.fluid) {
@@ -401,7 +402,7 @@ cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mo
                                 smem_sm / (int)(fa.sharedSizeBytes + 1024), 512 / TC_COLS});
             tc_cap = sms * std::max(occ, 1);
         }
-        const long nrows = (long)((a.W + D3_BLOCK - 1) / D3_BLOCK) * a.H * a.D;
+        const long nrows = ((long)a.W * a.H * a.D + D3_BLOCK - 1) / D3_BLOCK;
         const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
         if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
         else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
@@ -460,41 +461,83 @@ __global__ void filter_kernel(const float *rho, const float *ux, const float *uy
     out[9 * Nc + c] = (float)(syz / sr - by * bz);
 }
 
-// features and targets from the filtered fields (periodic central differences)
+// strain rate of the filtered velocity at coarse cell (I, J, K) (periodic
+// central differences) and the two contractions of the eddy-viscosity fit,
+// T_dev : S and S : S
+struct FilteredCell {
+    float S[3][3], TS, SS;
+    __device__ FilteredCell(const float *fl, int Wc, int Hc, int Dc, int I, int J, int K) {
+        const long Nc = (long)Wc * Hc * Dc;
+        auto at = [&](int i, int j, int k) -> long {
+            i = (i + Wc) % Wc; j = (j + Hc) % Hc; k = (k + Dc) % Dc;
+            return i + (long)Wc * (j + (long)Hc * k);
+        };
+        const long c = at(I, J, K);
+        const float *u[3] = {fl + Nc, fl + 2 * Nc, fl + 3 * Nc};
+        float du[3][3];  // du[a][b] = d u_b / d x_a
+        const long pa[3] = {at(I + 1, J, K), at(I, J + 1, K), at(I, J, K + 1)};
+        const long ma[3] = {at(I - 1, J, K), at(I, J - 1, K), at(I, J, K - 1)};
+        for (int aa = 0; aa < 3; aa++)
+            for (int b = 0; b < 3; b++) du[aa][b] = 0.5f * (u[b][pa[aa]] - u[b][ma[aa]]);
+        for (int aa = 0; aa < 3; aa++)
+            for (int b = 0; b < 3; b++) S[aa][b] = 0.5f * (du[aa][b] + du[b][aa]);
+        const float T[6] = {fl[4 * Nc + c], fl[5 * Nc + c], fl[6 * Nc + c],
+                            fl[7 * Nc + c], fl[8 * Nc + c], fl[9 * Nc + c]};
+        const float tr = (T[0] + T[1] + T[2]) / 3.f;
+        TS = (T[0] - tr) * S[0][0] + (T[1] - tr) * S[1][1] + (T[2] - tr) * S[2][2] +
+             2.f * (T[3] * S[0][1] + T[4] * S[0][2] + T[5] * S[1][2]);
+        SS = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2] +
+             2.f * (S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2]);
+    }
+};
+
+// T_dev : S and S : S of every coarse cell (for the averaged fit)
+__global__ void ts_ss_kernel(const float *fl, int Wc, int Hc, int Dc, float *ts, float *ss) {
+    const long Nc = (long)Wc * Hc * Dc;
+    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (c >= Nc) return;
+    const FilteredCell fc(fl, Wc, Hc, Dc, (int)(c % Wc), (int)((c / Wc) % Hc),
+                          (int)(c / ((long)Wc * Hc)));
+    ts[c] = fc.TS;
+    ss[c] = fc.SS;
+}
+
+// features and targets from the filtered fields.  The target is the eddy
+// viscosity of the least-squares fit of the sub-grid stress, nu_t =
+// max(0, -(T_dev : S) / (2 S : S)), either per cell (rad 0) or with both
+// contractions summed over the (2 rad + 1)^3 cells around it (periodic) before
+// the ratio is formed -- the averaging of the dynamic procedure, which leaves
+// far fewer cells clipped at zero and so does not bias the fit upward.
 __global__ void features_kernel(const float *fl, int Wc, int Hc, int Dc, float nu0, float s_ref,
-                                float z_max, float *feat, float *target) {
+                                float z_max, const float *ts, const float *ss, int rad,
+                                float *feat, float *target) {
     const long Nc = (long)Wc * Hc * Dc;
     const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (c >= Nc) return;
     const int I = (int)(c % Wc), J = (int)((c / Wc) % Hc), K = (int)(c / ((long)Wc * Hc));
-    auto at = [&](int i, int j, int k) -> long {
-        i = (i + Wc) % Wc; j = (j + Hc) % Hc; k = (k + Dc) % Dc;
-        return i + (long)Wc * (j + (long)Hc * k);
-    };
-    const float *u[3] = {fl + Nc, fl + 2 * Nc, fl + 3 * Nc};
-    float du[3][3];  // du[a][b] = d u_b / d x_a
-    const long pa[3] = {at(I + 1, J, K), at(I, J + 1, K), at(I, J, K + 1)};
-    const long ma[3] = {at(I - 1, J, K), at(I, J - 1, K), at(I, J, K - 1)};
-    for (int aa = 0; aa < 3; aa++)
-        for (int b = 0; b < 3; b++) du[aa][b] = 0.5f * (u[b][pa[aa]] - u[b][ma[aa]]);
-    float S[3][3];
-    for (int aa = 0; aa < 3; aa++)
-        for (int b = 0; b < 3; b++) S[aa][b] = 0.5f * (du[aa][b] + du[b][aa]);
-    const float T[6] = {fl[4 * Nc + c], fl[5 * Nc + c], fl[6 * Nc + c],
-                        fl[7 * Nc + c], fl[8 * Nc + c], fl[9 * Nc + c]};
-    const float tr = (T[0] + T[1] + T[2]) / 3.f;
-    const float TS = (T[0] - tr) * S[0][0] + (T[1] - tr) * S[1][1] + (T[2] - tr) * S[2][2] +
-                     2.f * (T[3] * S[0][1] + T[4] * S[0][2] + T[5] * S[1][2]);
-    const float SS = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2] +
-                     2.f * (S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2]);
+    const FilteredCell fc(fl, Wc, Hc, Dc, I, J, K);
+    float TS = fc.TS, SS = fc.SS;
+    if (rad > 0) {
+        double sts = 0.0, sss = 0.0;
+        for (int k = -rad; k <= rad; k++)
+            for (int j = -rad; j <= rad; j++)
+                for (int i = -rad; i <= rad; i++) {
+                    const long o = (I + i + Wc) % Wc +
+                                   (long)Wc * ((J + j + Hc) % Hc + (long)Hc * ((K + k + Dc) % Dc));
+                    sts += ts[o];
+                    sss += ss[o];
+                }
+        TS = (float)sts;
+        SS = (float)sss;
+    }
     const float nut = fmaxf(0.f, -TS / (2.f * SS + 1e-30f));
     target[c] = fminf(nut / nu0, z_max);
     float *fo = feat + c * MLP_IN;
     const float q = -2.f / s_ref;
     for (int i = 0; i < MLP_IN; i++) fo[i] = 0.f;
-    fo[3] = q * S[0][0]; fo[4] = q * S[1][1]; fo[5] = q * S[2][2];
-    fo[6] = q * S[0][1]; fo[7] = q * S[0][2]; fo[8] = q * S[1][2];
-    fo[18] = sqrtf(2.f * SS) / s_ref;
+    fo[3] = q * fc.S[0][0]; fo[4] = q * fc.S[1][1]; fo[5] = q * fc.S[2][2];
+    fo[6] = q * fc.S[0][1]; fo[7] = q * fc.S[0][2]; fo[8] = q * fc.S[1][2];
+    fo[18] = sqrtf(2.f * fc.SS) / s_ref;
 }
 
 // ------------------------------------------------------------------ training
@@ -860,7 +903,14 @@ int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, floa
 // nodes / factor^3) and the mean resolved kinetic energy of the filtered field
 int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
                       float *features_dev, float *targets_dev, double *ke_mean) {
-    if (!fine || factor < 1) return LB_ERR_ARG;
+    return lb_closure_sample_avg(fine, factor, nu0, s_ref, z_max, 0, features_dev, targets_dev,
+                                 ke_mean);
+}
+
+int lb_closure_sample_avg(lb_ctx *fine, int factor, float nu0, float s_ref, float z_max,
+                          int avg_radius, float *features_dev, float *targets_dev,
+                          double *ke_mean) {
+    if (!fine || factor < 1 || avg_radius < 0) return LB_ERR_ARG;
     float *f[4];
     int rc = lb_device_fields(fine, &f[0], &f[1], &f[2], &f[3]);
     if (rc != LB_OK) return rc;
@@ -871,16 +921,22 @@ int lb_closure_sample(lb_ctx *fine, int factor, float nu0, float s_ref, float z_
     const int Wc = W / factor, Hc = H / factor, Dc = D / factor;
     const long Nc = (long)Wc * Hc * Dc;
     float *fl = nullptr;
-    if (cudaMalloc(&fl, sizeof(float) * 10 * Nc) != cudaSuccess) return LB_ERR_NOMEM;
+    if (cudaMalloc(&fl, sizeof(float) * 12 * Nc) != cudaSuccess) return LB_ERR_NOMEM;
     cudaError_t e = cudaDeviceSynchronize();
     if (e == cudaSuccess) {
         filter_kernel<<<(unsigned)((Nc + 255) / 256), 256>>>(f[0], f[1], f[2], f[3], W, H, D,
                                                              factor, fl, Nc);
         e = cudaGetLastError();
     }
+    float *ts = fl + 10 * Nc, *ss = fl + 11 * Nc;
+    if (e == cudaSuccess && features_dev && targets_dev && avg_radius > 0) {
+        ts_ss_kernel<<<(unsigned)((Nc + 255) / 256), 256>>>(fl, Wc, Hc, Dc, ts, ss);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess && features_dev && targets_dev) {
         features_kernel<<<(unsigned)((Nc + 255) / 256), 256>>>(fl, Wc, Hc, Dc, nu0, s_ref, z_max,
-                                                               features_dev, targets_dev);
+                                                               ts, ss, avg_radius, features_dev,
+                                                               targets_dev);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && ke_mean) {

@@ -48,6 +48,16 @@ struct lb_ctx {
     int64_t launches = 0;
     int64_t steps = 0;                   // time steps since lb_create (or the checkpoint's)
     std::string err;
+    // z-slab of a larger lattice (lb_slab_create): planes 1..slab_nz are the
+    // global planes slab_z0 .. slab_z0 + slab_nz - 1; planes 0 and slab_nz + 1
+    // are ghost planes holding the neighbouring slabs' faces
+    int slab_nz = 0;                     // 0: not a slab
+    int slab_z0 = 0, slab_nz_global = 0;
+    cudaStream_t side = nullptr;         // the interior planes of a slab step
+    cudaEvent_t ev_in = nullptr, ev_done = nullptr, ev_pack = nullptr;
+    bool interior_pending = false;       // `side` holds interior planes `stream` has not joined
+    void *face[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // group exchange [parity][below/above]
+    int parity = 0;
 };
 
 namespace {
@@ -175,6 +185,14 @@ void drop_graphs(lb_ctx *c) {
         }
 }
 
+// a slab whose interior planes still run on the side stream: make the main
+// stream wait for them
+cudaError_t slab_join(lb_ctx *c) {
+    if (!c->interior_pending) return cudaSuccess;
+    c->interior_pending = false;
+    return cudaStreamWaitEvent(c->stream, c->ev_done, 0);
+}
+
 // after the stream has been synchronised: the device error word written by
 // the kernels that wait on the GPU (a persistent D2Q9 block that gave up
 // waiting for a neighbour band; a tcgen05 closure MMA that never completed)
@@ -215,28 +233,34 @@ D2Args d2_args(lb_ctx *c, int from) {
     return a;
 }
 
+// the D3Q19 kernel arguments of a step from set `from` into set 1-from
+D3Args d3_args(lb_ctx *c, int from) {
+    const lb_config &g = c->cfg;
+    D3Args a{};
+    for (int k = 0; k < 19; k++) {
+        a.src.f[k] = pop_k(c, from, k);
+        a.dst.f[k] = pop_k(c, 1 - from, k);
+    }
+    a.flags = c->flags; a.sb = c->sb;
+    a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
+    a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2); a.uz = mom_k(c, 3);
+    a.W = g.nx; a.H = g.ny; a.D = g.nz; a.dev = 0; a.ndev = 1;
+    a.w0 = (float)W3[0]; a.w1 = (float)W3[1]; a.w7 = (float)W3[2];
+    a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
+    a.Fx = g.force[0]; a.Fy = g.force[1]; a.Fz = g.force[2];
+    memcpy(a.corr, c->corr, sizeof(a.corr));
+    memcpy(a.wr, c->wr, sizeof(a.wr));
+    a.psi = c->sc; a.G = g.G; a.psi_form = g.psi_form;
+    a.probe = c->probe_o >= 0 ? c->probe_dev : nullptr;
+    a.probe_o = c->probe_o;
+    return a;
+}
+
 // one time step from set `from` into set 1-from
 cudaError_t step_once(lb_ctx *c, int from, bool moments) {
     const lb_config &g = c->cfg;
-    const int to = 1 - from;
     if (c->Q == 19) {
-        D3Args a{};
-        for (int k = 0; k < 19; k++) {
-            a.src.f[k] = pop_k(c, from, k);
-            a.dst.f[k] = pop_k(c, to, k);
-        }
-        a.flags = c->flags; a.sb = c->sb;
-        a.reverse = (c->tune & LB_TUNE_REVERSE) && from == 1;
-        a.rho = mom_k(c, 0); a.ux = mom_k(c, 1); a.uy = mom_k(c, 2); a.uz = mom_k(c, 3);
-        a.W = g.nx; a.H = g.ny; a.D = g.nz; a.dev = 0; a.ndev = 1;
-        a.w0 = (float)W3[0]; a.w1 = (float)W3[1]; a.w7 = (float)W3[2];
-        a.tau_inv = g.tau_inv; a.ux_in = g.u_in[0]; a.rho_out = g.rho_out;
-        a.Fx = g.force[0]; a.Fy = g.force[1]; a.Fz = g.force[2];
-        memcpy(a.corr, c->corr, sizeof(a.corr));
-        memcpy(a.wr, c->wr, sizeof(a.wr));
-        a.psi = c->sc; a.G = g.G; a.psi_form = g.psi_form;
-        a.probe = c->probe_o >= 0 ? c->probe_dev : nullptr;
-        a.probe_o = c->probe_o;
+        D3Args a = d3_args(c, from);
         if (g.mode == LB_MODE_REFERENCE) {
             c->launches += 1;
             return launch_d3q19_fused(a, MODE_REF, moments, false, c->stream);
@@ -461,8 +485,13 @@ int lb_destroy(lb_ctx *c) {
     if (c->red) cudaFree(c->red);
     if (c->psync) cudaFree(c->psync);
     if (c->probe_host) cudaFreeHost(c->probe_host);
-    if (c->ev0) cudaEventDestroy(c->ev0);
-    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->side) cudaStreamSynchronize(c->side);
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (c->face[i][j]) cudaFree(c->face[i][j]);
+    for (cudaEvent_t ev : {c->ev0, c->ev1, c->ev_in, c->ev_done, c->ev_pack})
+        if (ev) cudaEventDestroy(ev);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LB_OK;
@@ -511,6 +540,7 @@ int lb_set_populations(lb_ctx *c, const float *f) {
 
 int lb_get_populations(lb_ctx *c, float *f) {
     if (!c || !f) return fail(c, LB_ERR_ARG, "lb_get_populations: null argument");
+    LB_TRY(c, "lb_get_populations", slab_join(c));
     for (int k = 0; k < c->Q; k++) {
         const float *src = pop_k(c, c->cur, k);
         if (c->esize != 4) {
@@ -567,6 +597,9 @@ int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const floa
 
 int lb_step(lb_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return fail(c, LB_ERR_ARG, "lb_step: bad argument");
+    if (c->slab_nz)
+        return fail(c, LB_ERR_STATE, "lb_step: a slab steps with lb_slab_step or "
+                                     "lb_slab_group_step (its ghost planes need the exchange)");
     if (nsteps == 0) return LB_OK;
     if (persistent_on(c)) {
         // every step in one cooperative launch; falls through to the graphs
@@ -634,6 +667,7 @@ int lb_step(lb_ctx *c, int nsteps) {
 
 int lb_get_moments(lb_ctx *c, float *rho, float *ux, float *uy, float *uz) {
     if (!c) return LB_ERR_ARG;
+    LB_TRY(c, "lb_get_moments", slab_join(c));
     float *dst[4] = {rho, ux, uy, uz};
     for (int i = 0; i < 4; i++) {
         if (!dst[i] || (i == 3 && c->Q == 9)) continue;
@@ -647,10 +681,15 @@ int lb_get_moments(lb_ctx *c, float *rho, float *ux, float *uy, float *uz) {
 
 int lb_reduce(lb_ctx *c, double out[7]) {
     if (!c || !out) return LB_ERR_ARG;
+    LB_TRY(c, "lb_reduce", slab_join(c));
     double *res = c->red + reduce_partials_size();
+    // a slab sums its own planes only (not the ghost planes)
+    const long off = c->slab_nz ? (long)c->cfg.nx * c->cfg.ny : 0;
+    const long n = c->slab_nz ? off * c->slab_nz : c->N;
     LB_TRY(c, "lb_reduce",
-           launch_reduce(mom_k(c, 0), mom_k(c, 1), mom_k(c, 2), c->Q == 19 ? mom_k(c, 3) : nullptr,
-                         c->flags, CELL_WALL, c->N, c->red, res, c->stream));
+           launch_reduce(mom_k(c, 0) + off, mom_k(c, 1) + off, mom_k(c, 2) + off,
+                         c->Q == 19 ? mom_k(c, 3) + off : nullptr, c->flags + off, CELL_WALL, n,
+                         c->red, res, c->stream));
     c->launches += 2;
     LB_TRY(c, "lb_reduce", cudaMemcpyAsync(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
     LB_TRY(c, "lb_reduce", cudaStreamSynchronize(c->stream));
@@ -678,6 +717,7 @@ int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
     if (!c || !value || nsteps < 0) return LB_ERR_ARG;
     if (x < 0 || y < 0 || z < 0 || x >= c->cfg.nx || y >= c->cfg.ny || z >= c->cfg.nz)
         return fail(c, LB_ERR_ARG, "lb_run_probe: node outside the lattice");
+    if (c->slab_nz) return fail(c, LB_ERR_STATE, "lb_run_probe: not available on a slab");
     if (nsteps == 0) return LB_OK;
     if (probe_in_step(c)) {
         // every step's kernel writes the cursor node's moments into mapped
@@ -732,6 +772,7 @@ int lb_extents(const lb_ctx *c, int *nx, int *ny, int *nz) {
 
 int lb_synchronize(lb_ctx *c) {
     if (!c) return LB_ERR_ARG;
+    LB_TRY(c, "lb_synchronize", slab_join(c));
     LB_TRY(c, "lb_synchronize", cudaStreamSynchronize(c->stream));
     return check_persistent(c);
 }
@@ -862,6 +903,7 @@ extern "C" {
 
 int lb_checkpoint_save(lb_ctx *c, const char *path) {
     if (!c || !path) return fail(c, LB_ERR_ARG, "lb_checkpoint_save: null argument");
+    if (c->slab_nz) return fail(c, LB_ERR_STATE, "lb_checkpoint_save: not available on a slab");
     const long N = c->N;
     const size_t pop_k_bytes = (size_t)N * c->esize;
     CkptHeader h;
@@ -1024,6 +1066,246 @@ int lb_vtk_save_ctx(lb_ctx *c, const char *dir, int vtk_id) {
     return LB_OK;
 }
 
+}  // extern "C"
+
+// ----------------------------------------------------------------- z-slabs
+// The multi-device decomposition of a D3Q19 lattice (the reference's x-slab
+// halo exchange get_border -> copy_border -> apply_border,
+// src/get_border.cu:59-98, src/copy_border.cu:49-81, src/apply_border.cu:58-97,
+// driven from src/simulation_d3q19.cu:363-406), here along z, the slowest
+// axis, so that a face is contiguous: each of the 5 populations crossing a face
+// is one plane of its array.  Populations leaving through the upper face have
+// c_z = +1, through the lower face c_z = -1.
+namespace {
+
+const int kUp[5] = {5, 9, 13, 15, 17};     // c_z = +1
+const int kDown[5] = {6, 10, 14, 16, 18};  // c_z = -1
+
+long plane_of(const lb_ctx *c) { return (long)c->cfg.nx * c->cfg.ny; }
+
+void *plane_ptr(lb_ctx *c, int set, int k, int z) {
+    return static_cast<char *>((void *)pop_k(c, set, k)) + (size_t)z * plane_of(c) * c->esize;
+}
+
+// the faces of population set `set`: the c_z = -1 populations of plane 1 into
+// to_below, the c_z = +1 populations of plane slab_nz into to_above, each a
+// [5][nx * ny] array in the storage type
+cudaError_t slab_pack(lb_ctx *c, int set, void *to_below, void *to_above, cudaStream_t s) {
+    const void *src[10];
+    void *dst[10];
+    int n = 0;
+    const size_t pb = (size_t)plane_of(c) * c->esize;
+    for (int i = 0; i < 5; i++) {
+        if (to_below) {
+            src[n] = plane_ptr(c, set, kDown[i], 1);
+            dst[n++] = static_cast<char *>(to_below) + i * pb;
+        }
+        if (to_above) {
+            src[n] = plane_ptr(c, set, kUp[i], c->slab_nz);
+            dst[n++] = static_cast<char *>(to_above) + i * pb;
+        }
+    }
+    c->launches += n ? 1 : 0;
+    return launch_plane_copy(src, dst, n, (long)pb, s);
+}
+
+// the neighbours' faces into the ghost planes of set `set`: the lower
+// neighbour's upper face (c_z = +1) into plane 0, the upper neighbour's lower
+// face (c_z = -1) into plane slab_nz + 1
+cudaError_t slab_unpack(lb_ctx *c, int set, const void *from_below, const void *from_above,
+                        cudaStream_t s) {
+    const void *src[10];
+    void *dst[10];
+    int n = 0;
+    const size_t pb = (size_t)plane_of(c) * c->esize;
+    for (int i = 0; i < 5; i++) {
+        if (from_below) {
+            src[n] = static_cast<const char *>(from_below) + i * pb;
+            dst[n++] = plane_ptr(c, set, kUp[i], 0);
+        }
+        if (from_above) {
+            src[n] = static_cast<const char *>(from_above) + i * pb;
+            dst[n++] = plane_ptr(c, set, kDown[i], c->slab_nz + 1);
+        }
+    }
+    c->launches += n ? 1 : 0;
+    return launch_plane_copy(src, dst, n, (long)pb, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int lb_slab_create(const lb_config *global, int z0, int nz, lb_ctx **out) {
+    if (!global || !out) return LB_ERR_ARG;
+    *out = nullptr;
+    if (global->lattice != LB_D3Q19 || global->mode != LB_MODE_NATIVE || global->G != 0.f ||
+        nz < 1 || z0 < 0 || z0 + nz > global->nz) {
+        abi_record_error("lb_slab_create", "D3Q19 native mode without Shan-Chen, "
+                                           "0 <= z0 and z0 + nz <= the global nz");
+        return LB_ERR_ARG;
+    }
+    lb_config cfg = *global;
+    cfg.nz = nz + 2;  // the own planes and one ghost plane on each side
+    lb_ctx *c = nullptr;
+    int rc = lb_create(&cfg, &c);
+    if (rc != LB_OK) return rc;
+    c->slab_nz = nz;
+    c->slab_z0 = z0;
+    c->slab_nz_global = global->nz;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    for (cudaEvent_t *ev : {&c->ev_in, &c->ev_done, &c->ev_pack})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    const size_t fb = (size_t)5 * plane_of(c) * c->esize;
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            if (e == cudaSuccess) e = cudaMalloc(&c->face[i][j], fb);
+    if (e != cudaSuccess) {
+        lb_destroy(c);
+        return e == cudaErrorMemoryAllocation ? LB_ERR_NOMEM : LB_ERR_CUDA;
+    }
+    *out = c;
+    return LB_OK;
+}
+
+int lb_slab_info(const lb_ctx *c, int *z0, int *nz, int *nz_global, size_t *face_bytes) {
+    if (!c || !c->slab_nz) return LB_ERR_ARG;
+    if (z0) *z0 = c->slab_z0;
+    if (nz) *nz = c->slab_nz;
+    if (nz_global) *nz_global = c->slab_nz_global;
+    if (face_bytes) *face_bytes = (size_t)5 * plane_of(c) * c->esize;
+    return LB_OK;
+}
+
+void *lb_stream(lb_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int lb_slab_pack(lb_ctx *c, void *to_below, void *to_above) {
+    if (!c || !c->slab_nz) return fail(c, LB_ERR_ARG, "lb_slab_pack: not a slab");
+    LB_TRY(c, "lb_slab_pack", slab_join(c));
+    LB_TRY(c, "lb_slab_pack", slab_pack(c, c->cur, to_below, to_above, c->stream));
+    return LB_OK;
+}
+
+int lb_slab_step(lb_ctx *c, int moments, void *to_below, void *to_above) {
+    if (!c || !c->slab_nz) return fail(c, LB_ERR_ARG, "lb_slab_step: not a slab");
+    LB_TRY(c, "lb_slab_step", slab_join(c));
+    const int from = c->cur, to = 1 - from, nz = c->slab_nz;
+    const D3Args a = d3_args(c, from);
+    const bool mom = moments != 0;
+    // interior planes 2 .. nz - 1 on the side stream, after everything queued so far
+    if (nz > 2) {
+        LB_TRY(c, "lb_slab_step", cudaEventRecord(c->ev_in, c->stream));
+        LB_TRY(c, "lb_slab_step", cudaStreamWaitEvent(c->side, c->ev_in, 0));
+    }
+    // the two boundary planes 1 and nz first, then their faces, on the main stream
+    LB_TRY(c, "lb_slab_step", launch_d3q19_native_planes(a, c->cfg.storage, mom, 1, nz - 2,
+                                                         nz == 1 ? 1 : 2, c->stream));
+    c->launches += 1;
+    if (to_below || to_above)
+        LB_TRY(c, "lb_slab_step", slab_pack(c, to, to_below, to_above, c->stream));
+    if (nz > 2) {
+        LB_TRY(c, "lb_slab_step",
+               launch_d3q19_native_planes(a, c->cfg.storage, mom, 2, 0, nz - 2, c->side));
+        c->launches += 1;
+        LB_TRY(c, "lb_slab_step", cudaEventRecord(c->ev_done, c->side));
+        c->interior_pending = true;
+    }
+    c->cur = to;
+    c->steps += 1;
+    return LB_OK;
+}
+
+int lb_slab_unpack(lb_ctx *c, const void *from_below, const void *from_above) {
+    if (!c || !c->slab_nz) return fail(c, LB_ERR_ARG, "lb_slab_unpack: not a slab");
+    LB_TRY(c, "lb_slab_unpack", slab_unpack(c, c->cur, from_below, from_above, c->stream));
+    LB_TRY(c, "lb_slab_unpack", slab_join(c));
+    return LB_OK;
+}
+
+int lb_slab_group_step(lb_ctx *const *slabs, int n, int nsteps) {
+    if (!slabs || n < 1 || nsteps < 0) return LB_ERR_ARG;
+    int dev = -1;
+    for (int i = 0; i < n; i++) {
+        lb_ctx *c = slabs[i];
+        const lb_ctx *p = slabs[(i + n - 1) % n];
+        if (!c || !c->slab_nz || c->cfg.nx != slabs[0]->cfg.nx ||
+            c->cfg.ny != slabs[0]->cfg.ny || c->esize != slabs[0]->esize ||
+            c->slab_nz_global != slabs[0]->slab_nz_global ||
+            (p->slab_z0 + p->slab_nz) % c->slab_nz_global != c->slab_z0) {
+            abi_record_error("lb_slab_group_step", "slabs of one lattice, in z order, "
+                                                   "covering it without gaps");
+            return LB_ERR_ARG;
+        }
+    }
+    if (cudaGetDevice(&dev) != cudaSuccess) return LB_ERR_CUDA;
+    auto bad = [&](lb_ctx *c, cudaError_t e) {
+        cuda_fail(c, "lb_slab_group_step", e);
+        abi_record_error("lb_slab_group_step", c->err.c_str());
+        return LB_ERR_CUDA;
+    };
+    for (int t = 0; t < nsteps; t++) {
+        const bool last = t == nsteps - 1;
+        for (int i = 0; i < n; i++) {
+            lb_ctx *c = slabs[i];
+            int rc = lb_slab_step(c, last ? 1 : 0, c->face[c->parity][0], c->face[c->parity][1]);
+            if (rc != LB_OK) {
+                abi_record_error("lb_slab_group_step", c->err.c_str());
+                return rc;
+            }
+            cudaError_t e = cudaEventRecord(c->ev_pack, c->stream);
+            if (e != cudaSuccess) return bad(c, e);
+        }
+        for (int i = 0; i < n; i++) {
+            lb_ctx *c = slabs[i], *lo = slabs[(i + n - 1) % n], *hi = slabs[(i + 1) % n];
+            cudaError_t e = cudaSuccess;
+            if (lo != c) e = cudaStreamWaitEvent(c->stream, lo->ev_pack, 0);
+            if (e == cudaSuccess && hi != c && hi != lo)
+                e = cudaStreamWaitEvent(c->stream, hi->ev_pack, 0);
+            if (e != cudaSuccess) return bad(c, e);
+            int rc = lb_slab_unpack(c, lo->face[lo->parity][1], hi->face[hi->parity][0]);
+            if (rc != LB_OK) {
+                abi_record_error("lb_slab_group_step", c->err.c_str());
+                return rc;
+            }
+        }
+        // the next step packs into the other buffers: a slab's next pack then
+        // never overwrites a face its neighbours may still be reading
+        for (int i = 0; i < n; i++) slabs[i]->parity ^= 1;
+    }
+    return LB_OK;
+}
+
+int lb_slab_group_time(lb_ctx *const *slabs, int n, int nsteps, float *ms) {
+    if (!slabs || n < 1 || !ms || !slabs[0]) return LB_ERR_ARG;
+    lb_ctx *c0 = slabs[0];
+    // every slab starts after the start event and the stop event follows every slab
+    cudaError_t e = cudaEventRecord(c0->ev0, c0->stream);
+    for (int i = 1; i < n && e == cudaSuccess; i++)
+        e = cudaStreamWaitEvent(slabs[i]->stream, c0->ev0, 0);
+    if (e != cudaSuccess) {
+        abi_record_error("lb_slab_group_time", cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    int rc = lb_slab_group_step(slabs, n, nsteps);
+    if (rc != LB_OK) return rc;
+    for (int i = 1; i < n && e == cudaSuccess; i++) {
+        e = cudaEventRecord(slabs[i]->ev1, slabs[i]->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c0->stream, slabs[i]->ev1, 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c0->ev1, c0->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c0->ev1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, c0->ev0, c0->ev1);
+    if (e != cudaSuccess) {
+        abi_record_error("lb_slab_group_time", cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    return LB_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
 // ----------------------------------------------------------------- drop-in reductions
 // Scratch (first-pass partials + the 7 results) of the drop-in reductions,
 // one allocation per device ordinal, made on the first call with that device
@@ -1085,6 +1367,14 @@ int lb_device_count(int *n) {
     if (!n) return LB_ERR_ARG;
     return cudaGetDeviceCount(n) == cudaSuccess ? LB_OK : LB_ERR_CUDA;
 }
+int lb_set_device(int dev) {
+    const cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        abi_record_error("lb_set_device", cudaGetErrorString(e));
+        return e == cudaErrorInvalidDevice ? LB_ERR_ARG : LB_ERR_CUDA;
+    }
+    return LB_OK;
+}
 int lb_malloc(void **p, size_t bytes) {
     if (!p) return LB_ERR_ARG;
     return cudaMalloc(p, bytes) == cudaSuccess ? LB_OK : LB_ERR_NOMEM;
@@ -1115,7 +1405,7 @@ int lb_device_synchronize(void) {
 int lb::context_set_closure(lb_ctx *c, const ClosureArgs *ca) {
     if (!c) return LB_ERR_ARG;
     if (ca && (c->Q != 19 || c->cfg.mode != LB_MODE_NATIVE || c->cfg.storage != LB_STORE_F32 ||
-               sc_on(c)))
+               sc_on(c) || c->slab_nz))
         return fail(c, LB_ERR_ARG, "closure: D3Q19 native mode, FP32 storage, no Shan-Chen");
     LB_TRY(c, "closure", cudaStreamSynchronize(c->stream));
     drop_graphs(c);

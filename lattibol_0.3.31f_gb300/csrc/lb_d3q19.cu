@@ -458,6 +458,76 @@ static cudaError_t native_launch(const D3Args &a, bool mom, bool sc, cudaStream_
     return cudaGetLastError();
 }
 
+template <typename S>
+static cudaError_t native_planes(const D3Args &a0, bool mom, int z_lo, int z_skip, int nplanes,
+                                 cudaStream_t s) {
+    D3Args a = a0;
+    a.reverse = 0;
+    a.z_lo = z_lo;
+    a.z_skip = z_skip;
+    const dim3 g((a.W + D3_BLOCK - 1) / D3_BLOCK, a.H, nplanes), b(D3_BLOCK);
+    if (mom) d3q19_fused_kernel<MODE_NATIVE, true, false, S, false><<<g, b, 0, s>>>(a);
+    else d3q19_fused_kernel<MODE_NATIVE, false, false, S, false><<<g, b, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_d3q19_native_planes(const D3Args &a, int storage, bool mom, int z_lo,
+                                       int z_skip, int nplanes, cudaStream_t s) {
+    if (nplanes <= 0) return cudaSuccess;
+    switch (storage) {
+    case 0: return native_planes<float>(a, mom, z_lo, z_skip, nplanes, s);
+    case 1: return native_planes<__half>(a, mom, z_lo, z_skip, nplanes, s);
+    case 2: return native_planes<__nv_bfloat16>(a, mom, z_lo, z_skip, nplanes, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// Plane copies of the z-slab exchange: up to 10 planes (the 5 populations
+// crossing each of a slab's two faces) in one launch; blockIdx.y picks the
+// plane, the x blocks stride through its bytes.  The pointers may lie on
+// another device the calling one reaches (peer loads or stores).
+// ---------------------------------------------------------------------------
+constexpr int PC_MAX = 10;
+struct PlaneCopyArgs {
+    const char *src[PC_MAX];
+    char *dst[PC_MAX];
+    long n;  // elements of T per plane
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) plane_copy_kernel(const PlaneCopyArgs p) {
+    const T *src = reinterpret_cast<const T *>(p.src[blockIdx.y]);
+    T *dst = reinterpret_cast<T *>(p.dst[blockIdx.y]);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < p.n;
+         i += (long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+cudaError_t launch_plane_copy(const void *const *src, void *const *dst, int n, long bytes,
+                              cudaStream_t s) {
+    if (n <= 0 || bytes <= 0) return cudaSuccess;
+    if (n > PC_MAX) return cudaErrorInvalidValue;
+    PlaneCopyArgs p{};
+    uintptr_t align = (uintptr_t)bytes;
+    for (int i = 0; i < n; i++) {
+        p.src[i] = static_cast<const char *>(src[i]);
+        p.dst[i] = static_cast<char *>(dst[i]);
+        align |= (uintptr_t)src[i] | (uintptr_t)dst[i];
+    }
+    const int w = (align & 15) == 0 ? 16 : (align & 3) == 0 ? 4 : (align & 1) == 0 ? 2 : 1;
+    p.n = bytes / w;
+    const long per = (p.n + 255) / 256;
+    const dim3 g((unsigned)(per < 64 ? (per > 0 ? per : 1) : 64), n);
+    switch (w) {
+    case 16: plane_copy_kernel<uint4><<<g, 256, 0, s>>>(p); break;
+    case 4: plane_copy_kernel<uint32_t><<<g, 256, 0, s>>>(p); break;
+    case 2: plane_copy_kernel<uint16_t><<<g, 256, 0, s>>>(p); break;
+    default: plane_copy_kernel<uint8_t><<<g, 256, 0, s>>>(p); break;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc, cudaStream_t s) {
     switch (storage) {
     case 0: return native_launch<float>(a, mom, sc, s);

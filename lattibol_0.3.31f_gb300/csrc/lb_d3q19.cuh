@@ -34,7 +34,7 @@ struct Coord3 {
         const int bx = a.reverse ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
         x = bx * blockDim.x + threadIdx.x;
         y = a.reverse ? a.H - 1 - (int)blockIdx.y : (int)blockIdx.y;
-        z = a.reverse ? a.D - 1 - (int)blockIdx.z : (int)blockIdx.z;
+        z = a.reverse ? a.D - 1 - (int)blockIdx.z : a.z_lo + (int)blockIdx.z * (1 + a.z_skip);
     }
 };
 

@@ -31,6 +31,8 @@ struct D3Args {
     float4 *probe;          // when set: (ux, uy, uz, rho) of node probe_o, every step
     int probe_o;            // (mapped host memory: the cursor read without a sync)
     int *err;               // device error word of a kernel that waits on the GPU (or null)
+    int z_lo, z_skip;       // planes updated: z = z_lo + blockIdx.z * (1 + z_skip) (slabs;
+                            // 0, 0 = every plane, blockIdx.z itself)
 };
 
 struct D2Args {
@@ -55,6 +57,14 @@ cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, c
 // native mode with storage kind (0 f32, 1 f16, 2 bf16) and optional Shan-Chen
 // (sc: the density pass writing a.psi, then the fused step reading it)
 cudaError_t launch_d3q19_native(const D3Args &a, int storage, bool mom, bool sc, cudaStream_t s);
+// the native step (no Shan-Chen) of `nplanes` planes z = z_lo + i * (1 + z_skip),
+// i < nplanes, of a z-slab whose ghost planes hold the neighbours' faces
+cudaError_t launch_d3q19_native_planes(const D3Args &a, int storage, bool mom, int z_lo,
+                                       int z_skip, int nplanes, cudaStream_t s);
+// copies n planes of `bytes` bytes each from src[i] to dst[i] (any devices the
+// calling one can reach); 16-byte accesses when every pointer and `bytes` allow
+cudaError_t launch_plane_copy(const void *const *src, void *const *dst, int n, long bytes,
+                              cudaStream_t s);
 // single-pass Shan-Chen step (psi halo in shared memory, z-marching tiles);
 // usable when sc_march_chunk(W, H, D) != 0
 int sc_march_chunk(int W, int H, int D);

@@ -86,9 +86,11 @@ def box_filter(rho, ux, uy, uz, W, H, D, fac):
     return sr / fac ** 3, ub, T
 
 
-def features_targets(ub, T, nu0, s_ref, z_max):
+def features_targets(ub, T, nu0, s_ref, z_max, avg_radius=0):
     """The closure's training features [Nc][19] and targets z = nu_t/nu0 from
-    filtered fields on a periodic coarse grid (axes z, y, x)."""
+    filtered fields on a periodic coarse grid (axes z, y, x).  avg_radius > 0:
+    T_dev : S and S : S summed over the (2 r + 1)^3 cells around each cell
+    before nu_t is formed (the target of lb_closure_sample_avg)."""
     def d(a, axis):  # derivative along lattice axis (0 = x, 1 = y, 2 = z)
         ax = {0: 2, 1: 1, 2: 0}[axis]
         return 0.5 * (np.roll(a, -1, ax) - np.roll(a, 1, ax))
@@ -99,7 +101,12 @@ def features_targets(ub, T, nu0, s_ref, z_max):
           + 2 * (T[3] * S[0][1] + T[4] * S[0][2] + T[5] * S[1][2]))
     SS = (S[0][0] ** 2 + S[1][1] ** 2 + S[2][2] ** 2
           + 2 * (S[0][1] ** 2 + S[0][2] ** 2 + S[1][2] ** 2))
-    nut = np.maximum(0.0, -TS / (2 * SS + 1e-30))
+    TSa, SSa = TS, SS
+    if avg_radius > 0:
+        rr = range(-avg_radius, avg_radius + 1)
+        TSa = sum(np.roll(TS, (k, j, i), (0, 1, 2)) for k in rr for j in rr for i in rr)
+        SSa = sum(np.roll(SS, (k, j, i), (0, 1, 2)) for k in rr for j in rr for i in rr)
+    nut = np.maximum(0.0, -TSa / (2 * SSa + 1e-30))
     z = np.minimum(nut / nu0, z_max).reshape(-1)
     n = z.size
     F = np.zeros((n, IN))
