@@ -195,6 +195,10 @@ typedef enum {
                                    single-pass step whose populations arrive in
                                    shared memory by asynchronous copies issued
                                    ahead of use; part of the default */
+#define LB_TUNE_SC_NO_TMA 0x080 /* staged Shan-Chen step, 16-bit storage: copy
+                                   every stage with 16-byte cp.async chunks, also
+                                   where TMA tensor copies could (the interior
+                                   tiles); same results (FP32 always uses cp.async) */
 #define LB_TUNE_TBLOCK_SHAPE(n) ((n) << 12) /* with LB_TUNE_TBLOCK: block shape 1..10
                                                (steps per launch x tile), 0 = the
                                                library's choice */

@@ -97,6 +97,7 @@ LB_TUNE_DEFAULT, LB_TUNE_EXPLICIT, LB_TUNE_REVERSE, LB_TUNE_SC_SINGLE_PASS = 0, 
 LB_TUNE_PERSISTENT, LB_TUNE_PDL, LB_TUNE_CLOSURE_MMA_SYNC = 0x004, 0x008, 0x010
 LB_TUNE_TBLOCK = 0x020
 LB_TUNE_SC_STAGED = 0x040
+LB_TUNE_SC_NO_TMA = 0x080
 
 
 def LB_TUNE_TBLOCK_SHAPE(n):

@@ -83,14 +83,20 @@ __device__ __forceinline__ int wrap_add(int v, int c, int n) {
 __device__ __forceinline__ float ld_stream(const float *p) { return __ldg(p); }
 
 // Population storage.  FP32 stores f_k itself.  The 16-bit forms store the
-// deviation f_k - wr_k from an offset wr_k = w_k * rho_ref (rounded to float
-// once on the host); the arithmetic stays FP32: load = wr_k + widen(h),
-// store = narrow_rne(f_k - wr_k).
+// deviation d_k = f_k - wr_k from an offset wr_k = w_k * rho_ref (rounded to
+// float once on the host), widened to FP32 for the arithmetic.  load/store
+// convert between f and the stored form (f = wr_k + widen(h), h =
+// narrow_rne(f - wr_k): lb_set/get_populations, equilibrium initialisation).
+// The step kernels keep the value their arithmetic works on: f itself in
+// FP32, the widened deviation d_k in 16-bit storage (load_dev / store_dev,
+// no offset added or taken off; the d3q19_*_dev arithmetic below).
 template <typename S> struct Store;
 template <> struct Store<float> {
     static constexpr int kind = 0;
     __device__ __forceinline__ static float load(const float *p, float) { return __ldg(p); }
     __device__ __forceinline__ static void store(float *p, float v, float) { *p = v; }
+    __device__ __forceinline__ static float load_dev(const float *p) { return __ldg(p); }
+    __device__ __forceinline__ static void store_dev(float *p, float v) { *p = v; }
 };
 template <> struct Store<__half> {
     static constexpr int kind = 1;
@@ -100,6 +106,12 @@ template <> struct Store<__half> {
     __device__ __forceinline__ static void store(__half *p, float v, float wr) {
         *p = __float2half_rn(v - wr);
     }
+    __device__ __forceinline__ static float load_dev(const __half *p) {
+        return __half2float(__ldg(p));
+    }
+    __device__ __forceinline__ static void store_dev(__half *p, float d) {
+        *p = __float2half_rn(d);
+    }
 };
 template <> struct Store<__nv_bfloat16> {
     static constexpr int kind = 2;
@@ -108,6 +120,12 @@ template <> struct Store<__nv_bfloat16> {
     }
     __device__ __forceinline__ static void store(__nv_bfloat16 *p, float v, float wr) {
         *p = __float2bfloat16_rn(v - wr);
+    }
+    __device__ __forceinline__ static float load_dev(const __nv_bfloat16 *p) {
+        return __bfloat162float(__ldg(p));
+    }
+    __device__ __forceinline__ static void store_dev(__nv_bfloat16 *p, float d) {
+        *p = __float2bfloat16_rn(d);
     }
 };
 
@@ -225,6 +243,74 @@ __device__ __forceinline__ void d3q19_bgk_native(float (&g)[19], float ux, float
     pair(10, 13, a7, ux - uz);
     pair(15, 18, a7, uy + uz);
     pair(16, 17, a7, uy - uz);
+}
+
+// ----------------------------------- 16-bit storage: arithmetic on deviations
+// The state is d_k = f_k - wr_k with wr_k = w_k rho_ref.  Density: rho =
+// rho_ref + sum_k d_k (the native moments' association over d; rho_ref here
+// is sum_k wr_k, the density the offsets carry, rounded once); momentum
+// sum_k c_k d_k (the offsets cancel pairwise: wr_k = wr_opp(k) exactly).
+// Relaxation: d_k' = (1 - tau_inv) d_k + tau_inv (f_eq,k - wr_k), evaluated
+// per opposite pair as x = fma(tau_inv w rho, q, -tau_inv wr), d' =
+// fma(1 - tau_inv, d, x): as many instructions as the FP32 form, no offset
+// added on load or taken off on store, and f_eq - wr formed with one
+// rounding (no cancellation against wr).
+__device__ __forceinline__ float d3q19_rho_dev(const float (&d)[19], float rho_ref) {
+    return rho_ref + d3q19_rho_native(d);
+}
+
+__device__ __forceinline__ void d3q19_moments_dev(const float (&d)[19], float rho_ref,
+                                                  float &rho, float &ux, float &uy, float &uz) {
+    float px, mx, zx;
+    d3q19_xsums_native(d, px, mx, zx);
+    rho = rho_ref + ((px + mx) + zx);
+    const float jy = ((d[3] + d[7]) + (d[11] + d[15]) + d[16]) -
+                     ((d[4] + d[8]) + (d[12] + d[17]) + d[18]);
+    const float jz = ((d[5] + d[9]) + (d[13] + d[15]) + d[17]) -
+                     ((d[6] + d[10]) + (d[14] + d[16]) + d[18]);
+    const float inv = 1.f / rho;
+    ux = (px - mx) * inv;
+    uy = jy * inv;
+    uz = jz * inv;
+}
+
+// one opposite pair of the deviation BGK: t = fma(4.5p, p, base), q+- =
+// fma(+-3, p, t), x+- = fma(oa, q+-, -owr), d+- = fma(om, d+-, x+-), the pair
+// in paired FP32 FMAs (each lane the scalar IEEE fma)
+__device__ __forceinline__ void bgk_pair_dev(float2 &dd, float oa, float owr, float p, float base,
+                                             float om) {
+    const float t = __fmaf_rn(4.5f * p, p, base);
+    const float2 q = __ffma2_rn(make_float2(3.f, -3.f), make_float2(p, p), make_float2(t, t));
+    const float2 x = __ffma2_rn(make_float2(oa, oa), q, make_float2(-owr, -owr));
+    dd = __ffma2_rn(make_float2(om, om), dd, x);
+}
+
+// deviation BGK at velocity (ux, uy, uz); wr0, wr1, wr7: the offsets of the
+// three weight classes
+__device__ __forceinline__ void d3q19_bgk_dev(float (&d)[19], float ux, float uy, float uz,
+                                              float rho, float w0, float w1, float w7,
+                                              float tau_inv, float wr0, float wr1, float wr7) {
+    const float usq = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, ux * ux));
+    const float base = __fmaf_rn(-1.5f, usq, 1.f);
+    const float om = 1.f - tau_inv;
+    const float oa0 = tau_inv * (w0 * rho), oa1 = tau_inv * (w1 * rho), oa7 = tau_inv * (w7 * rho);
+    const float owr0 = tau_inv * wr0, owr1 = tau_inv * wr1, owr7 = tau_inv * wr7;
+    d[0] = __fmaf_rn(om, d[0], __fmaf_rn(oa0, base, -owr0));
+    auto pair = [&](int kp, int km, float oa, float owr, float p) {
+        float2 dd = make_float2(d[kp], d[km]);
+        bgk_pair_dev(dd, oa, owr, p, base, om);
+        d[kp] = dd.x;
+        d[km] = dd.y;
+    };
+    pair(1, 2, oa1, owr1, ux);
+    pair(3, 4, oa1, owr1, uy);
+    pair(5, 6, oa1, owr1, uz);
+    pair(7, 12, oa7, owr7, ux + uy);
+    pair(8, 11, oa7, owr7, ux - uy);
+    pair(9, 14, oa7, owr7, ux + uz);
+    pair(10, 13, oa7, owr7, ux - uz);
+    pair(15, 18, oa7, owr7, uy + uz);
+    pair(16, 17, oa7, owr7, uy - uz);
 }
 
 // Shan-Chen interaction sum over the 18 neighbours, ps[k] = psi(x + c_k):

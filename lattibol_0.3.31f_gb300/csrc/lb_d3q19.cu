@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
             d3q19_zou_he_east(g, a.rho_out);
     }
     float rho, ux, uy, uz;
-    if (MODE == MODE_NATIVE) d3q19_moments_native(g, rho, ux, uy, uz);
+    if (MODE == MODE_NATIVE) StepArith<S>::moments(g, a, rho, ux, uy, uz);
     else d3q19_moments(g, rho, ux, uy, uz);
     if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
     if (PLOT) a.plot[o] = make_float4(ux, uy, uz, rho);
@@ -105,13 +105,13 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
                 ez = __fmaf_rn(c, IFz, ez);
             }
         }
-        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+        StepArith<S>::bgk(g, ex, ey, ez, rho, a, a.tau_inv);
     } else {
         d3q19_bgk(g, ux, uy, uz, rho, a.w0, a.w1, a.w7, a.tau_inv);
     }
     S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
-    for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], a.wr[k]);
+    for (int k = 0; k < 19; k++) Store<S>::store_dev(dst[k] + o, g[k]);
 }
 
 // Density pass of the Shan-Chen step: psi(rho) of the post-stream density of
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a)
     const Nbr3 n(c.x, c.y, c.z, a.W, a.H, a.D);
     float g[19];
     pull_native<S>(a, o, n, fl, g);
-    const float rho = d3q19_rho_native(g);
+    const float rho = StepArith<S>::rho(g, a);
     a.psi[o] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
@@ -162,7 +162,7 @@ __device__ __forceinline__ float sc_psi_of_node(const D3Args &a, int x, int y, i
     const Nbr3 n(x, y, zz, a.W, a.H, a.D);
     float g[19];
     pull_native<S>(a, o, n, fl, g);
-    const float rho = d3q19_rho_native(g);
+    const float rho = StepArith<S>::rho(g, a);
     return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(SC_THREADS, 4) d3q19_sc_march_kernel(const D3A
             float g[19];
             const Nbr3 n(x, y, zz, a.W, a.H, a.D);
             pull_native<S>(a, o, n, fl, g);
-            const float rho = d3q19_rho_native(g);
+            const float rho = StepArith<S>::rho(g, a);
             psi = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 #pragma unroll
             for (int k = 0; k < 19; k++) sg[zl & 1][k][tid] = g[k];
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(SC_THREADS, 4) d3q19_sc_march_kernel(const D3A
 #pragma unroll
             for (int k = 0; k < 19; k++) g[k] = sg[z & 1][k][tid];
             float rho, ux, uy, uz;
-            d3q19_moments_native(g, rho, ux, uy, uz);
+            StepArith<S>::moments(g, a, rho, ux, uy, uz);
             if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
             if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
             const float inv_rt = 1.f / (rho * a.tau_inv);
@@ -235,10 +235,10 @@ __global__ void __launch_bounds__(SC_THREADS, 4) d3q19_sc_march_kernel(const D3A
             ex = __fmaf_rn(c, IFx, ex);
             ey = __fmaf_rn(c, IFy, ey);
             ez = __fmaf_rn(c, IFz, ez);
-            d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, a.tau_inv);
+            StepArith<S>::bgk(g, ex, ey, ez, rho, a, a.tau_inv);
             S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
 #pragma unroll
-            for (int k = 0; k < 19; k++) Store<S>::store(dst[k] + o, g[k], a.wr[k]);
+            for (int k = 0; k < 19; k++) Store<S>::store_dev(dst[k] + o, g[k]);
         } else {
             if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
             if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);

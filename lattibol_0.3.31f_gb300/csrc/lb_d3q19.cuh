@@ -38,7 +38,8 @@ struct Coord3 {
     }
 };
 
-// Native pull of the 19 populations of fluid node o (see d3q19_fused_kernel).
+// Native pull of the 19 populations of fluid node o (see d3q19_fused_kernel):
+// f_k in FP32 storage, the deviation d_k in 16-bit storage.
 template <typename S>
 __device__ __forceinline__ void pull_native(const D3Args &a, int o, const Nbr3 &n, uint8_t fl,
                                             float (&g)[19]) {
@@ -49,16 +50,16 @@ __device__ __forceinline__ void pull_native(const D3Args &a, int o, const Nbr3 &
             const int up = o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k));
             const uint8_t fu = k == 0 ? 0 : a.flags[up];
             if (fu & CELL_WALL) {
-                const float v = Store<S>::load(src[d3_opp(k)] + o, a.wr[d3_opp(k)]);
+                const float v = Store<S>::load_dev(src[d3_opp(k)] + o);
                 g[k] = (fu & CELL_MOVING) ? v - a.corr[d3_opp(k)] : v;
             } else {
-                g[k] = Store<S>::load(src[k] + up, a.wr[k]);
+                g[k] = Store<S>::load_dev(src[k] + up);
             }
         }
     } else {
 #pragma unroll
         for (int k = 0; k < 19; k++)
-            g[k] = Store<S>::load(src[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)), a.wr[k]);
+            g[k] = Store<S>::load_dev(src[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)));
     }
 }
 

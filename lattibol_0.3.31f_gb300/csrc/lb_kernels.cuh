@@ -3,6 +3,8 @@
 // (lb_abi.cu, lb_context.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include "lb_common.cuh"
 #include "lb_mlp.cuh"
 
@@ -33,7 +35,39 @@ struct D3Args {
     int *err;               // device error word of a kernel that waits on the GPU (or null)
     int z_lo, z_skip;       // planes updated: z = z_lo + blockIdx.z * (1 + z_skip) (slabs;
                             // 0, 0 = every plane, blockIdx.z itself)
+    float rho_ref;          // 16-bit storage: sum_k wr[k], the density the offsets carry
 };
+
+// The native step's arithmetic for storage type S: FP32 works on f itself,
+// 16-bit storage on the deviations d_k = f_k - w_k rho_ref (lb_common.cuh).
+template <typename S> struct StepArith {
+    __device__ __forceinline__ static float rho(const float (&g)[19], const D3Args &) {
+        return d3q19_rho_native(g);
+    }
+    __device__ __forceinline__ static void moments(const float (&g)[19], const D3Args &,
+                                                   float &rho, float &ux, float &uy, float &uz) {
+        d3q19_moments_native(g, rho, ux, uy, uz);
+    }
+    __device__ __forceinline__ static void bgk(float (&g)[19], float ux, float uy, float uz,
+                                               float rho, const D3Args &a, float tau_inv) {
+        d3q19_bgk_native(g, ux, uy, uz, rho, a.w0, a.w1, a.w7, tau_inv);
+    }
+};
+template <typename S> struct StepArithDev {
+    __device__ __forceinline__ static float rho(const float (&d)[19], const D3Args &a) {
+        return d3q19_rho_dev(d, a.rho_ref);
+    }
+    __device__ __forceinline__ static void moments(const float (&d)[19], const D3Args &a,
+                                                   float &rho, float &ux, float &uy, float &uz) {
+        d3q19_moments_dev(d, a.rho_ref, rho, ux, uy, uz);
+    }
+    __device__ __forceinline__ static void bgk(float (&d)[19], float ux, float uy, float uz,
+                                               float rho, const D3Args &a, float tau_inv) {
+        d3q19_bgk_dev(d, ux, uy, uz, rho, a.w0, a.w1, a.w7, tau_inv, a.wr[0], a.wr[1], a.wr[7]);
+    }
+};
+template <> struct StepArith<__half> : StepArithDev<__half> {};
+template <> struct StepArith<__nv_bfloat16> : StepArithDev<__nv_bfloat16> {};
 
 struct D2Args {
     CPop<9> src;
@@ -74,7 +108,13 @@ cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaSt
 // sc_stage_chunk(W, H, D) != 0.  A block that gives up waiting for its copies
 // sets *a.err (when a.err is set).
 int sc_stage_chunk(int W, int H, int D);
-cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom, cudaStream_t s);
+// tmap: the tensor map of a.src (sc_stage_tensor_map) for the blocks whose
+// stages lie inside the lattice, or null (every stage by cp.async chunks)
+cudaError_t launch_d3q19_sc_stage(const D3Args &a, int storage, bool mom,
+                                  const CUtensorMap *tmap, cudaStream_t s);
+// the tensor map the staged step reads a.src through; false if it cannot be
+// encoded (no driver entry point, or a layout it does not describe)
+bool sc_stage_tensor_map(const D3Args &a, int storage, CUtensorMap *out);
 // self-check of the staged step's bounded wait: one block whose first stage
 // waits get no polls gives up, sets *err (device memory) and returns
 cudaError_t sc_stage_wait_selftest(int *err);

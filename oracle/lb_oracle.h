@@ -57,6 +57,10 @@ void lbo_d3q19_stream_native_##S(R *f, const uint8_t *flags, const R *corr, int 
 void lbo_d3q19_collide_native_##S(R *f, const uint8_t *flags, R *ux, R *uy, R *uz,        \
     R *rho, R *psi, int W, int H, int D, R w0, R w1, R w7, R tau_inv, R Fx, R Fy, R Fz,   \
     R G, int psi_form);                                                                   \
+/* 16-bit storage: the same step on the deviations d_k = f_k - wr_k */                  \
+void lbo_d3q19_collide_native_dev_##S(R *d, const uint8_t *flags, R *ux, R *uy, R *uz,    \
+    R *rho, R *psi, int W, int H, int D, R w0, R w1, R w7, R tau_inv, R Fx, R Fy, R Fz,   \
+    R G, int psi_form, R rho_off, const R *wr);                                           \
 void lbo_d2q9_stream_native_##S(R *f, const uint8_t *flags, const R *corr, int W, int H); \
 void lbo_d2q9_collide_native_##S(R *f, const uint8_t *flags, R *ux, R *uy, R *rho,        \
     R *psi, int W, int H, R w0, R w1, R w5, R tau_inv, R Fx, R Fy, R G, R Gads,           \

@@ -240,6 +240,52 @@ def storage_offsets(lattice, rho_ref=1.0):
     return np.array([np.float32(wk * r) for wk in w], np.float32)
 
 
+# ---- 16-bit storage as the library's step kernels keep it: the deviations
+# d_k = f_k - wr_k themselves (the step's arithmetic works on d, lb_common.cuh
+# d3q19_*_dev), narrowed and widened on every store and load
+
+def rho_offset(wr):
+    """The density the offsets carry, sum_k wr_k in double rounded to float."""
+    return np.float32(np.sum(np.asarray(wr, np.float64)))
+
+
+def to_dev(f, wr, kind):
+    """The stored deviations of a float population state: widen(narrow(f -
+    wr)) for every node (lb_set_populations)."""
+    d = np.ascontiguousarray(np.asarray(f, np.float32) - np.asarray(wr, np.float32)[:, None])
+    lib().lbo_round_storage(_p(d), ctypes.c_long(d.size), kind)
+    return d
+
+
+def from_dev(d, wr):
+    """Float populations wr + d (lb_get_populations)."""
+    return np.asarray(wr, np.float32)[:, None] + d
+
+
+def quantize(d, kind, flags=None):
+    """In place: d = widen(narrow(d)) on non-wall nodes (a step's stores)."""
+    assert d.dtype == np.float32 and d.flags.c_contiguous
+    if flags is None:
+        lib().lbo_round_storage(_p(d), ctypes.c_long(d.size), kind)
+        return
+    fluid = (np.asarray(flags) & SOLID) == 0
+    q = np.ascontiguousarray(d[:, fluid])
+    lib().lbo_round_storage(_p(q), ctypes.c_long(q.size), kind)
+    d[:, fluid] = q
+
+
+def d3q19_collide_native_dev(d, flags, mom, W, H, D, w0, w1, w7, tau_inv, wr, F=(0, 0, 0),
+                             G=0.0, psi=None, psi_form=PSI_EXP1):
+    """The native collision on the deviation state d of 16-bit storage (float)."""
+    assert d.dtype == np.float32
+    c = ctypes.c_float
+    wr = np.ascontiguousarray(wr, np.float32)
+    ux, uy, uz, rho = mom if mom is not None else (None,) * 4
+    lib().lbo_d3q19_collide_native_dev_f32(
+        _p(d), _p(flags), _p(ux), _p(uy), _p(uz), _p(rho), _p(psi), W, H, D, c(w0), c(w1),
+        c(w7), c(tau_inv), c(F[0]), c(F[1]), c(F[2]), c(G), psi_form, c(rho_offset(wr)), _p(wr))
+
+
 def quantize_dev(f, wr, flags=None, kind=1):
     """In place: f[k] = wr[k] + widen(narrow(f[k] - wr[k])) on non-wall nodes
     (kind 1 = binary16, 2 = bfloat16)."""

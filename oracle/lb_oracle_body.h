@@ -140,6 +140,52 @@ static inline void FN(d3q19_bgk_native)(R *g, R ux, R uy, R uz, R rho, R w0, R w
     FN(bgk_pair_native)(g, 15, 18, a7, uy + uz, base, tau_inv);
     FN(bgk_pair_native)(g, 16, 17, a7, uy - uz, base, tau_inv);
 }
+/* 16-bit storage: the step on the deviations d_k = f_k - wr_k
+ * (lattibol_0.3.31f_gb300/csrc/lb_common.cuh, d3q19_*_dev): density
+ * rho_off + sum d (rho_off = sum_k wr_k), momentum sum c d, relaxation
+ * d' = fma(1 - tau_inv, d, fma(tau_inv w rho, q, -tau_inv wr)) */
+static inline void FN(d3q19_moments_dev)(const R *d, R rho_off, R *rho, R *ux, R *uy, R *uz)
+{
+    R px, mx, zx;
+    FN(d3q19_xsums_native)(d, &px, &mx, &zx);
+    const R r = rho_off + ((px + mx) + zx);
+    const R jy = ((d[3] + d[7]) + (d[11] + d[15]) + d[16]) -
+                 ((d[4] + d[8]) + (d[12] + d[17]) + d[18]);
+    const R jz = ((d[5] + d[9]) + (d[13] + d[15]) + d[17]) -
+                 ((d[6] + d[10]) + (d[14] + d[16]) + d[18]);
+    const R inv = (R)1 / r;
+    *rho = r;
+    *ux = (px - mx) * inv;
+    *uy = jy * inv;
+    *uz = jz * inv;
+}
+static inline void FN(bgk_pair_dev)(R *d, int kp, int km, R oa, R owr, R p, R base, R om)
+{
+    const R t = FMA_R((R)4.5f * p, p, base);
+    const R xp = FMA_R(oa, FMA_R((R)3.f, p, t), -owr);
+    const R xm = FMA_R(oa, FMA_R((R)-3.f, p, t), -owr);
+    d[kp] = FMA_R(om, d[kp], xp);
+    d[km] = FMA_R(om, d[km], xm);
+}
+static inline void FN(d3q19_bgk_dev)(R *d, R ux, R uy, R uz, R rho, R w0, R w1, R w7,
+                                     R tau_inv, R wr0, R wr1, R wr7)
+{
+    const R usq = FMA_R(uz, uz, FMA_R(uy, uy, ux * ux));
+    const R base = FMA_R((R)-1.5f, usq, (R)1.f);
+    const R om = (R)1.f - tau_inv;
+    const R oa0 = tau_inv * (w0 * rho), oa1 = tau_inv * (w1 * rho), oa7 = tau_inv * (w7 * rho);
+    const R owr0 = tau_inv * wr0, owr1 = tau_inv * wr1, owr7 = tau_inv * wr7;
+    d[0] = FMA_R(om, d[0], FMA_R(oa0, base, -owr0));
+    FN(bgk_pair_dev)(d, 1, 2, oa1, owr1, ux, base, om);
+    FN(bgk_pair_dev)(d, 3, 4, oa1, owr1, uy, base, om);
+    FN(bgk_pair_dev)(d, 5, 6, oa1, owr1, uz, base, om);
+    FN(bgk_pair_dev)(d, 7, 12, oa7, owr7, ux + uy, base, om);
+    FN(bgk_pair_dev)(d, 8, 11, oa7, owr7, ux - uy, base, om);
+    FN(bgk_pair_dev)(d, 9, 14, oa7, owr7, ux + uz, base, om);
+    FN(bgk_pair_dev)(d, 10, 13, oa7, owr7, ux - uz, base, om);
+    FN(bgk_pair_dev)(d, 15, 18, oa7, owr7, uy + uz, base, om);
+    FN(bgk_pair_dev)(d, 16, 17, oa7, owr7, uy - uz, base, om);
+}
 /* native D2Q9 (lattibol_0.3.31f_gb300/csrc/lb_common.cuh, d2q9_*_native):
  * partial sums by c_x, one division for 1/rho, the BGK pairs above */
 static inline void FN(d2q9_moments_native)(const R *g, R *rho, R *ux, R *uy)
@@ -513,9 +559,13 @@ void FN(lbo_d3q19_stream_native)(R *f, const uint8_t *flags, const R *corr, int 
 /* Native collision: local swap, moments, body-force velocity shift (the form
  * of src/collision.cu:280-284), optional Shan-Chen force on the 18-neighbour
  * stencil (psi of the post-stream density), BGK.  Moment pointers may be NULL. */
-void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *uz, R *rho,
-                                  R *psi, int W, int H, int D, R w0, R w1, R w7, R tau_inv,
-                                  R Fx, R Fy, R Fz, R G, int psi_form)
+/* dev != 0: f holds the deviations d_k = f_k - wr_k of 16-bit storage and the
+ * step uses the deviation arithmetic (wr: per-direction offsets, rho_off =
+ * their sum) */
+static void FN(d3q19_collide_native_impl)(R *f, const uint8_t *flags, R *ux, R *uy, R *uz,
+                                          R *rho, R *psi, int W, int H, int D, R w0, R w1,
+                                          R w7, R tau_inv, R Fx, R Fy, R Fz, R G, int psi_form,
+                                          int dev, R rho_off, const R *wr)
 {
     const long N = (long)W * H * D;
     const int sc = (G != 0) && psi;
@@ -528,7 +578,8 @@ void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *u
             R g[19];
             g[0] = f[o];
             for (int k = 1; k < 19; k++) g[k] = f[D3_OPP[k] * N + o];
-            psi[o] = FN(psi_of)(FN(d3q19_rho_native)(g), psi_form);
+            const R r = dev ? rho_off + FN(d3q19_rho_native)(g) : FN(d3q19_rho_native)(g);
+            psi[o] = FN(psi_of)(r, psi_form);
         }
     }
 #pragma omp parallel for schedule(static)
@@ -544,7 +595,8 @@ void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *u
             R t = g[k]; g[k] = g[q]; g[q] = t;
         }
         R r, vx, vy, vz;
-        FN(d3q19_moments_native)(g, &r, &vx, &vy, &vz);
+        if (dev) FN(d3q19_moments_dev)(g, rho_off, &r, &vx, &vy, &vz);
+        else FN(d3q19_moments_native)(g, &r, &vx, &vy, &vz);
         R ex = vx, ey = vy, ez = vz;
         if (sc || Fx != 0 || Fy != 0 || Fz != 0) {
             const R inv_rt = (R)1 / (r * tau_inv);
@@ -566,9 +618,27 @@ void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *u
             }
         }
         if (rho) { ux[o] = vx; uy[o] = vy; uz[o] = vz; rho[o] = r; }
-        FN(d3q19_bgk_native)(g, ex, ey, ez, r, w0, w1, w7, tau_inv);
+        if (dev) FN(d3q19_bgk_dev)(g, ex, ey, ez, r, w0, w1, w7, tau_inv, wr[0], wr[1], wr[7]);
+        else FN(d3q19_bgk_native)(g, ex, ey, ez, r, w0, w1, w7, tau_inv);
         for (int k = 0; k < 19; k++) f[k * N + o] = g[k];
     }
+}
+
+void FN(lbo_d3q19_collide_native)(R *f, const uint8_t *flags, R *ux, R *uy, R *uz, R *rho,
+                                  R *psi, int W, int H, int D, R w0, R w1, R w7, R tau_inv,
+                                  R Fx, R Fy, R Fz, R G, int psi_form)
+{
+    FN(d3q19_collide_native_impl)(f, flags, ux, uy, uz, rho, psi, W, H, D, w0, w1, w7, tau_inv,
+                                  Fx, Fy, Fz, G, psi_form, 0, (R)0, NULL);
+}
+
+void FN(lbo_d3q19_collide_native_dev)(R *d, const uint8_t *flags, R *ux, R *uy, R *uz, R *rho,
+                                      R *psi, int W, int H, int D, R w0, R w1, R w7, R tau_inv,
+                                      R Fx, R Fy, R Fz, R G, int psi_form, R rho_off,
+                                      const R *wr)
+{
+    FN(d3q19_collide_native_impl)(d, flags, ux, uy, uz, rho, psi, W, H, D, w0, w1, w7, tau_inv,
+                                  Fx, Fy, Fz, G, psi_form, 1, rho_off, wr);
 }
 
 void FN(lbo_d2q9_stream_native)(R *f, const uint8_t *flags, const R *corr, int W, int H)

@@ -8,6 +8,10 @@ lattices without wall nodes.
   (ny = 8), and the march runs over several z chunks (the chunk length is
   the shortest that divides nz when the lattice is small), with a body force
   and graph-replayed batches whose last step writes the moments.
+* Tiles away from the lattice's edges get their stages by TMA tensor copies,
+  edge tiles (periodic wrap) by cp.async chunks: the same lattices with every
+  stage copied by cp.async give the same bits, and so do lattices of 3 x 3
+  and 5 x 5 tiles per plane against the two-pass step.
 * Bit-exact against the float oracle on its own.
 * A lattice with a wall node takes the two-pass step whatever the tuning
   says (two launches per step), and returns to the staged step when the
@@ -18,12 +22,15 @@ import ctypes
 import numpy as np
 import pytest
 
+from storage_emul import Emulated
+
 from conftest import load_package
 from golden_io import bits
 
 pytestmark = pytest.mark.gpu
 
 STAGED = 0x100 | 0x040   # LB_TUNE_EXPLICIT | LB_TUNE_SC_STAGED
+NO_TMA = 0x080           # LB_TUNE_SC_NO_TMA: every stage by cp.async chunks
 TWO_PASS = 0x100         # LB_TUNE_EXPLICIT
 
 
@@ -63,8 +70,8 @@ def run(pkg, shape, storage, tuning, steps, flags=None, seed=3, graph_steps=4):
     return out
 
 
-@pytest.mark.parametrize("shape", [(32, 8, 8), (64, 16, 48), (96, 24, 20)],
-                         ids=["32x8x8", "64x16x48", "96x24x20"])
+@pytest.mark.parametrize("shape", [(32, 8, 8), (64, 16, 48), (96, 24, 20), (160, 40, 16)],
+                         ids=["32x8x8", "64x16x48", "96x24x20", "160x40x16"])
 @pytest.mark.parametrize("storage", [0, 1, 2], ids=["f32", "f16", "bf16"])
 def test_staged_matches_two_pass(pkg, shape, storage):
     steps = 14
@@ -77,9 +84,22 @@ def test_staged_matches_two_pass(pkg, shape, storage):
         assert beq(a, b)
 
 
+@pytest.mark.parametrize("shape", [(96, 24, 20), (160, 40, 16), (256, 64, 8)],
+                         ids=["3x3_tiles", "5x5_tiles", "8x8_tiles"])
+@pytest.mark.parametrize("storage", [0, 1, 2], ids=["f32", "f16", "bf16"])
+def test_tma_tiles_match_cp_async_tiles(pkg, shape, storage):
+    f_t, m_t, l_t = run(pkg, shape, storage, STAGED, 11)
+    f_c, m_c, l_c = run(pkg, shape, storage, STAGED | NO_TMA, 11)
+    assert l_t == l_c == 11
+    assert np.isfinite(f_t).all()
+    assert beq(f_t, f_c)
+    for a, b in zip(m_t, m_c):
+        assert beq(a, b)
+
+
 @pytest.mark.parametrize("storage", [0, 2], ids=["f32", "bf16"])
 def test_staged_vs_oracle(pkg, oracle, storage):
-    W, H, D = 64, 16, 12
+    W, H, D = 128, 32, 12   # 4 x 4 tiles per plane: the middle four by TMA
     N = W * H * D
     steps = 10
     F = (np.float32(2e-6), np.float32(0), np.float32(-1e-6))
@@ -87,20 +107,13 @@ def test_staged_vs_oracle(pkg, oracle, storage):
     rho = spinodal(N, 11)
     z = np.zeros(N, np.float32)
     flags = np.zeros(N, np.uint8)
-    f = oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3)
-    wr = oracle.storage_offsets(19, 0.693)
-    if storage:
-        oracle.quantize_dev(f, wr, None, storage)
+    em = Emulated(oracle, oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3), storage, 0.693)
     mom = [np.zeros(N, np.float32) for _ in range(4)]
     psi = np.zeros(N, np.float32)
     zc = np.zeros(19, np.float32)
     for _ in range(steps):
-        oracle.d3q19_stream_native(f, flags, zc, W, H, D)
-        oracle.d3q19_collide_native(f, flags, mom, W, H, D, *pkg.W3, np.float32(1.0), F,
-                                    G=-5.0, psi=psi, psi_form=oracle.PSI_EXP1)
-        if storage:
-            oracle.quantize_dev(f, wr, None, storage)
-    assert beq(f_g, f)
+        em.step(flags, zc, W, H, D, mom, pkg.W3, np.float32(1.0), F, G=-5.0, psi=psi)
+    assert beq(f_g, em.populations())
     rho_g, ux_g, uy_g, uz_g = m_g
     assert beq(rho_g, mom[3]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1]) and beq(uz_g, mom[2])
 

@@ -1,8 +1,9 @@
 """GPU parity of the 16-bit deviation storage and of the D3Q19 Shan-Chen step.
 
 * FP16 / BF16 storage without Shan-Chen is bit-exact against the oracle with
-  the storage emulated (each value kept as w_k*rho_ref + widen(narrow(f -
-  w_k*rho_ref)), computed in float exactly like the kernel's load/store).
+  the storage emulated (the deviations d_k = f_k - w_k*rho_ref stepped with
+  the deviation arithmetic, narrowed and widened on every store, exactly like
+  the kernels' loads and stores).
 * Shan-Chen (psi = 1 - exp(-rho), exp evaluated by the library's own float
   function on both sides) is bit-exact too, through both the single-pass
   z-marching kernel and the separate psi pass.
@@ -17,6 +18,7 @@ import pytest
 
 from conftest import load_package
 from golden_io import bits
+from storage_emul import Emulated
 
 pytestmark = pytest.mark.gpu
 
@@ -60,19 +62,15 @@ def test_deviation_storage_bitexact(pkg, oracle, storage, kind):
     lat.set_flags(flags)
     f0 = oracle.d3q19_equilibrium(rho, ux, z, z, *pkg.W3)
     lat.set_populations(f0)
-    wr = oracle.storage_offsets(19, rho_ref)
-    f = f0.copy()
-    oracle.quantize_dev(f, wr, flags, kind)
+    em = Emulated(oracle, f0, kind, rho_ref)
     fluid = (flags & 1) == 0
-    assert beq(lat.populations()[:, fluid], f[:, fluid])   # set/get round trip
+    assert beq(lat.populations()[:, fluid], em.populations()[:, fluid])   # set/get round trip
     lat.step(25)
     corr = oracle.wall_correction(19, (0.03, 0, 0))
     mom = [np.zeros(N, np.float32) for _ in range(4)]
     for _ in range(25):
-        oracle.d3q19_stream_native(f, flags, corr, W, H, D)
-        oracle.d3q19_collide_native(f, flags, mom, W, H, D, *pkg.W3, tau_inv, F)
-        oracle.quantize_dev(f, wr, flags, kind)
-    assert beq(lat.populations()[:, fluid], f[:, fluid])
+        em.step(flags, corr, W, H, D, mom, pkg.W3, tau_inv, F)
+    assert beq(lat.populations()[:, fluid], em.populations()[:, fluid])
     # moments read after the populations: the conversions must not touch them
     rho_g, ux_g, uy_g, uz_g = lat.moments()
     assert beq(rho_g, mom[3]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1])
@@ -117,25 +115,18 @@ def test_shan_chen_d3q19_vs_oracle(pkg, oracle, storage):
                       storage=storage, rho_ref=0.693)
     lat.set_flags(flags)
     lat.init_equilibrium(rho, z, z, z)
-    f = oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3)
-    wr = oracle.storage_offsets(19, 0.693)
-    if storage:
-        oracle.quantize_dev(f, wr, None, storage)
+    em = Emulated(oracle, oracle.d3q19_equilibrium(rho, z, z, z, *pkg.W3), storage, 0.693)
     lat.step(40)
     mom = [np.zeros(N, np.float32) for _ in range(4)]
     psi = np.zeros(N, np.float32)
     zc = np.zeros(19, np.float32)
     for _ in range(40):
-        oracle.d3q19_stream_native(f, flags, zc, n, n, n)
-        oracle.d3q19_collide_native(f, flags, mom, n, n, n, *pkg.W3, np.float32(1.0), G=-5.0,
-                                    psi=psi, psi_form=oracle.PSI_EXP1)
-        if storage:
-            oracle.quantize_dev(f, wr, None, storage)
+        em.step(flags, zc, n, n, n, mom, pkg.W3, np.float32(1.0), G=-5.0, psi=psi)
     rho_g, ux_g, uy_g, uz_g = lat.moments()
     assert beq(rho_g, mom[3])
     for a, b in zip((ux_g, uy_g, uz_g), mom[:3]):
         assert beq(a, b)
-    assert beq(lat.populations(), f)
+    assert beq(lat.populations(), em.populations())
     lat.close()
 
 
@@ -269,21 +260,15 @@ def test_shan_chen_paths_with_walls_vs_oracle(pkg, oracle, tuning, storage):
     lat.set_flags(flags)
     f = oracle.d3q19_equilibrium(rho, zero, zero, zero, *pkg.W3)
     lat.set_populations(f)
-    wr = oracle.storage_offsets(19, 0.693)
-    if storage:
-        oracle.quantize_dev(f, wr, flags, storage)
+    em = Emulated(oracle, f, storage, 0.693)
     lat.step(12)
     corr = oracle.wall_correction(19, (0.02, 0, 0))
     mom = [np.zeros(N, np.float32) for _ in range(4)]
     psi = np.zeros(N, np.float32)
     for _ in range(12):
-        oracle.d3q19_stream_native(f, flags, corr, W, H, D)
-        oracle.d3q19_collide_native(f, flags, mom, W, H, D, *pkg.W3, np.float32(1.0), F,
-                                    G=-5.0, psi=psi, psi_form=oracle.PSI_EXP1)
-        if storage:
-            oracle.quantize_dev(f, wr, flags, storage)
+        em.step(flags, corr, W, H, D, mom, pkg.W3, np.float32(1.0), F, G=-5.0, psi=psi)
     fluid = (flags & 1) == 0
-    assert beq(lat.populations()[:, fluid], f[:, fluid])
+    assert beq(lat.populations()[:, fluid], em.populations()[:, fluid])
     rho_g, ux_g, uy_g, uz_g = lat.moments()
     assert beq(rho_g, mom[3]) and beq(uz_g, mom[2])
     lat.close()

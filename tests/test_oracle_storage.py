@@ -63,3 +63,36 @@ def test_quantize_dev_keeps_walls(oracle):
     d = (f[:, flags == 0] - wr[:, None]).astype(np.float32)
     exp = (wr[:, None] + d.astype(np.float16).astype(np.float32)).astype(np.float32)
     assert np.array_equal(g[:, flags == 0], exp)
+
+
+def test_deviation_step_tracks_the_float_step(oracle):
+    """The deviation form of the native collision (16-bit storage's
+    arithmetic, no narrowing here) gives the float step's populations,
+    moments and psi to FP32 rounding: the offsets carry rho_ref exactly."""
+    W, H, D = 12, 10, 8
+    N = W * H * D
+    rng = np.random.default_rng(3)
+    rho = (0.693 * (1 + 0.01 * rng.uniform(-1, 1, N))).astype(np.float32)
+    u = [(0.02 * rng.standard_normal(N)).astype(np.float32) for _ in range(3)]
+    w = (np.float32(1 / 3), np.float32(1 / 18), np.float32(1 / 36))
+    f = oracle.d3q19_equilibrium(rho, *u, *w)
+    wr = oracle.storage_offsets(19, 0.693)
+    d = np.ascontiguousarray(f - wr[:, None])
+    flags = np.zeros(N, np.uint8)
+    zc = np.zeros(19, np.float32)
+    F = (np.float32(1e-5), np.float32(0), np.float32(0))
+    m_f = [np.zeros(N, np.float32) for _ in range(4)]
+    m_d = [np.zeros(N, np.float32) for _ in range(4)]
+    psi_f, psi_d = np.zeros(N, np.float32), np.zeros(N, np.float32)
+    for tau_inv in (np.float32(1.0), np.float32(1 / 0.7)):
+        for _ in range(5):
+            oracle.d3q19_stream_native(f, flags, zc, W, H, D)
+            oracle.d3q19_collide_native(f, flags, m_f, W, H, D, *w, tau_inv, F, G=-5.0, psi=psi_f)
+            oracle.d3q19_stream_native(d, flags, zc, W, H, D)
+            oracle.d3q19_collide_native_dev(d, flags, m_d, W, H, D, *w, tau_inv, wr, F, G=-5.0,
+                                            psi=psi_d)
+        np.testing.assert_allclose(oracle.from_dev(d, wr), f, rtol=0, atol=2e-7)
+        for a, b in zip(m_d, m_f):
+            np.testing.assert_allclose(a, b, rtol=0, atol=2e-6)
+        np.testing.assert_allclose(psi_d, psi_f, rtol=0, atol=1e-6)
+    assert oracle.rho_offset(wr) == np.float32(np.sum(wr.astype(np.float64)))
