@@ -522,9 +522,10 @@ def main():
         f16 = measure_f16(pkg, wl, flags, args, ws, dist, glups)
 
     # ------------------------------------------------ end to end through the C ABI
-    e2e = None
+    e2e = e2e_dropin = None
     if args.e2e_steps > 0 and wl.name == "channel":
         e2e = measure_e2e(pkg, L, wl, flags, args.e2e_steps, ws, dist)
+        e2e_dropin = measure_e2e_dropin(pkg, L, wl, flags, max(200, args.e2e_steps // 4))
 
     if rank != 0:
         return 0
@@ -550,6 +551,8 @@ def main():
         line["fp16_storage"] = f16
     if e2e:
         line["e2e"] = e2e
+    if e2e_dropin:
+        line["e2e_dropin"] = e2e_dropin
     if not args.no_cpu_baseline and ws == 1:
         cb = cpu_baseline(wl, budget_s=float(os.environ.get("LB_CPU_BUDGET_S", "12")))
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -687,6 +690,87 @@ def measure_f16(pkg, wl, flags, args, ws, dist, glups_f32):
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "bytes_per_lu": 77}}
+
+
+def solid_bound_d3q19(solid, nx, ny, nz):
+    """The reference's solid_bound rule (src/simulation_d3q19.cu:167-204): a
+    solid node whose 18 neighbours are all solid, for x in 1 .. nx-2 only,
+    y and z periodic."""
+    s = solid.reshape(nz, ny, nx).astype(bool)
+    sb = s.copy()
+    for cz in (-1, 0, 1):
+        for cy in (-1, 0, 1):
+            for cx in (-1, 0, 1):
+                if abs(cx) + abs(cy) + abs(cz) in (1, 2):
+                    sb &= np.roll(s, (-cz, -cy, -cx), (0, 1, 2))
+    sb[:, :, 0] = sb[:, :, -1] = False
+    return sb.reshape(-1).astype(np.uint8)
+
+
+def measure_e2e_dropin(pkg, L, wl, flags, steps, fused=True):
+    """The reference's own host sequence through the drop-in entry points, on
+    the headline lattice in the reference's semantics: lb_run_lbm_d3q19 runs,
+    per step, streaming_d3q19, collision_d3q19 into the plot buffer (Zou-He
+    velocity inlet u = 0 at x = 0 and pressure outlet rho = 1 at x = nx-1,
+    full-way bounce-back walls and sphere), read_value_3d at the cursor and a
+    16-byte device-to-host copy, as SimulationD3Q19::runLBM does
+    (src/simulation_d3q19.cu:350-430).  tau = 0.8: at 0.55 the reference's
+    own Zou-He faces grow a disturbance on this geometry (the oracle, the
+    reference compiled for the host, does the same).  Timed with host
+    buffers: the populations uploaded from pinned memory, the run, and the
+    moment fields read back."""
+    import ctypes as C
+    nx, ny, nz = wl.size
+    N = wl.N
+    solid = (flags & 1).astype(np.uint8)
+    sb = solid_bound_d3q19(solid, nx, ny, nz)
+    dd = pkg.DeviceData(19, nx, ny, nz, plot=True)
+    dd.set_solid(solid, sb)
+    hp = C.c_void_p()
+    assert L.lb_malloc_host(C.byref(hp), 4 * 19 * N) == 0
+    f_host = np.frombuffer((C.c_float * (19 * N)).from_address(hp.value), np.float32).reshape(19, N)
+    for k in range(19):
+        f_host[k] = pkg.W3[0] if k == 0 else (pkg.W3[1] if k <= 6 else pkg.W3[2])
+    mp = C.c_void_p()
+    assert L.lb_malloc_host(C.byref(mp), 4 * 4 * N) == 0
+    m_host = np.frombuffer((C.c_float * (4 * N)).from_address(mp.value), np.float32).reshape(4, N)
+    vp = C.c_void_p()
+    assert L.lb_malloc_host(C.byref(vp), 16) == 0
+    prm = pkg.abi.lb_run_params_d3q19()
+    prm.w0, prm.w1, prm.w7 = (float(w) for w in pkg.W3)
+    prm.tau_inv, prm.rho_out = np.float32(1 / 0.8), 1.0
+    prm.cursor[0], prm.cursor[1], prm.cursor[2] = nx // 2, ny // 3, nz // 2
+    L.lb_abi_set_mode(pkg.abi.LB_ABI_FUSED if fused else pkg.abi.LB_ABI_STANDALONE)
+
+    def run(n):
+        for k, name in enumerate(dd.s.POP):
+            assert L.lb_memcpy_h2d(C.c_void_p(getattr(dd.s, name)),
+                                   C.c_void_p(hp.value + 4 * k * N), 4 * N) == 0
+        rc = L.lb_run_lbm_d3q19(dd.ptr(), C.c_void_p(dd.plot), C.byref(prm), n, vp)
+        assert rc == 0, L.lb_abi_last_error()
+        for i, name in enumerate(("rho", "ux", "uy", "uz")):
+            assert L.lb_memcpy_d2h(C.c_void_p(mp.value + 4 * i * N),
+                                   C.c_void_p(getattr(dd.s, name)), 4 * N) == 0
+
+    run(3)
+    launches_before = None
+    t0 = time.perf_counter()
+    run(steps)
+    el = time.perf_counter() - t0
+    assert np.isfinite(m_host[0]).all()
+    L.lb_abi_release_d3q19(dd.ptr())
+    L.lb_abi_set_mode(pkg.abi.LB_ABI_STANDALONE)
+    dd.close()
+    for p_ in (hp, mp, vp):
+        L.lb_free_host(p_)
+    del launches_before
+    return {"value": N * steps / el / 1e9, "unit": "GLUPS", "steps": steps,
+            "h2d_bytes_per_step": 4 * 19 * N / steps, "d2h_bytes_per_step": (16 * steps + 16 * N) / steps,
+            "mode": "fused" if fused else "standalone",
+            "path": "lb_run_lbm_d3q19: per step streaming_d3q19 + collision_d3q19 (plot buffer) "
+                    "+ read_value_3d + a 16-byte synchronous copy to pinned host memory; the "
+                    "reference's semantics (Zou-He x faces, full-way bounce-back), tau 0.8",
+            "bytes_per_lu": 185 if fused else 330}
 
 
 def measure_e2e(pkg, L, wl, flags, steps, ws, dist):

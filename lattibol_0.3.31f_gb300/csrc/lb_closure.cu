@@ -19,6 +19,7 @@
 //   backward pass per sample, per-block weight-gradient sums in shared
 //   memory, a fixed-order reduction of the block partials, and Adam.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -543,26 +544,46 @@ __global__ void features_kernel(const float *fl, int Wc, int Hc, int Dc, float n
 // ------------------------------------------------------------------ training
 constexpr int HROW = MLP_H + 1;
 struct TrainSmemWarp {
-    MlpSmemWarp m;
-    float h2[32 * HROW];   // row stride 65: a warp walking its rows hits 32 banks
+    MlpSmemWarp m;                         // x and the first hidden layer (BF16), y
+    float h2[32 * HROW];                   // row stride 65: a warp walking its rows hits 32 banks
     float dh2[32 * HROW];
     float dh1[32 * HROW];
+    __nv_bfloat16 dh2b[32 * SH_STRIDE];    // BF16 copies: operands of the gradient MMAs
+    __nv_bfloat16 dh1b[32 * SH_STRIDE];
     float dy[32];
 };
 constexpr int TRAIN_WARPS = 4;
 constexpr int NGRAD = MLP_NPARAM + 1;  // + loss
+// the per-warp tiles start on a 128-byte boundary after the weights
+constexpr size_t TRAIN_WARP_OFF = (sizeof(MlpSmemWeights) + 127) / 128 * 128;
 constexpr size_t TRAIN_SMEM =
-    sizeof(MlpSmemWeights) + TRAIN_WARPS * sizeof(TrainSmemWarp) + NGRAD * sizeof(float);
+    TRAIN_WARP_OFF + TRAIN_WARPS * sizeof(TrainSmemWarp) + NGRAD * sizeof(float);
+static_assert(offsetof(MlpSmemWeights, w2) % 16 == 0 && sizeof(MlpSmemWarp) % 16 == 0 &&
+                  (32 * HROW * sizeof(float)) % 16 == 0 && sizeof(TrainSmemWarp) % 16 == 0,
+              "ldmatrix rows stay 16-byte aligned");
 
-// forward (tensor cores, as in the closure kernel) + FP32 backward over the
-// samples [0, n) of a batch; each block leaves its gradient sums (already
-// divided by n) and its loss sum in partial[block][NGRAD]
+// Forward (mma.sync, as mlp_forward_warp) and backward over the samples
+// [0, n) of a batch, every contraction on the tensor cores (mma.sync
+// m16n8k16, BF16 operands, FP32 accumulate).  A block takes 128 samples at a
+// time, 32 per warp:
+//  * per warp: dy = 2 (y - z) / n per sample, dH2 = dy w3 (h2 > 0) from the
+//    second layer's accumulator fragments, dH1 = (dH2 W2) (h1 > 0) -- dH2 and
+//    W2 as BF16 operands (W2 read transposed by ldmatrix .trans);
+//  * per block (after a barrier): warp w owns rows 16w .. 16w+15 of dW2 =
+//    dH2^T H1 and of dW1 = dH1^T X, contracting over all 128 samples in a
+//    fixed order (both operands read transposed by ldmatrix .trans), and adds
+//    them into the block's gradient sums, every element owned by one thread;
+//  * the bias and output-layer gradients (db1, db2, dw3, db3) are FP32 sums
+//    over the samples, each parameter owned by one thread.
+// Rounding points (restated by the numpy oracle): dH2 and dH1 enter the MMAs
+// as BF16; everything is accumulated in FP32.  Each block leaves its gradient
+// sums (already divided by n) and its loss sum in partial[block][NGRAD].
 __global__ void __launch_bounds__(32 * TRAIN_WARPS) mlp_train_kernel(
     MlpDev mlp, const float *X, const float *Z, long n, float *partial) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     MlpSmemWeights &sW = *reinterpret_cast<MlpSmemWeights *>(smem);
-    TrainSmemWarp *sWarp = reinterpret_cast<TrainSmemWarp *>(smem + sizeof(MlpSmemWeights));
-    float *sG = reinterpret_cast<float *>(smem + sizeof(MlpSmemWeights) +
+    TrainSmemWarp *sWarp = reinterpret_cast<TrainSmemWarp *>(smem + TRAIN_WARP_OFF);
+    float *sG = reinterpret_cast<float *>(smem + TRAIN_WARP_OFF +
                                           TRAIN_WARPS * sizeof(TrainSmemWarp));
     mlp_load_weights(sW, mlp);
     for (int i = threadIdx.x; i < NGRAD; i += blockDim.x) sG[i] = 0.f;
@@ -570,6 +591,12 @@ __global__ void __launch_bounds__(32 * TRAIN_WARPS) mlp_train_kernel(
     TrainSmemWarp &tw = sWarp[wid];
     const int g = lane >> 2, t = lane & 3;
     const float inv_n = 1.f / (float)n;
+    // ldmatrix row addresses: (row, column) of this lane in the four 8x8 matrices
+    // of a 16x16 tile read as [k-rows 0-7 | 8-15] x [n-columns 0-7 | 8-15]
+    const int lr_b = (lane & 7) + 8 * ((lane >> 3) & 1), lc_b = 8 * (lane >> 4);
+    //   ... and as [m-columns 0-7 | 8-15] x [k-rows 0-7 | 8-15] (A from a stored
+    //   [k][m] matrix)
+    const int lr_a = (lane & 7) + 8 * (lane >> 4), lc_a = 8 * ((lane >> 3) & 1);
     __syncthreads();
     for (long base = (long)blockIdx.x * 32 * TRAIN_WARPS; base < n;
          base += (long)gridDim.x * 32 * TRAIN_WARPS) {
@@ -580,63 +607,155 @@ __global__ void __launch_bounds__(32 * TRAIN_WARPS) mlp_train_kernel(
                 __float2bfloat16_rn((valid && i < MLP_IN) ? X[s * MLP_IN + i] : 0.f);
         float h2[2][8][4];
         mlp_forward_warp(sW, tw.m, h2, true);
-        // scatter the second hidden layer to rows
+        const float err = valid ? tw.m.y[lane] - Z[s] : 0.f;
+        tw.dy[lane] = 2.f * err * inv_n;
+        __syncwarp();
+        // dH2 = dy w3 (h2 > 0), from the accumulator fragments
 #pragma unroll
-        for (int mt = 0; mt < 2; mt++)
+        for (int mt = 0; mt < 2; mt++) {
+            const int r0 = mt * 16 + g, r1 = r0 + 8;
+            const float dy0 = tw.dy[r0], dy1 = tw.dy[r1];
 #pragma unroll
             for (int nt = 0; nt < 8; nt++) {
-                const int c0 = nt * 8 + 2 * t, r0 = mt * 16 + g;
-                tw.h2[r0 * HROW + c0] = h2[mt][nt][0];
-                tw.h2[r0 * HROW + c0 + 1] = h2[mt][nt][1];
-                tw.h2[(r0 + 8) * HROW + c0] = h2[mt][nt][2];
-                tw.h2[(r0 + 8) * HROW + c0 + 1] = h2[mt][nt][3];
+                const int c0 = nt * 8 + 2 * t;
+                const float *q = h2[mt][nt];
+                const float d00 = q[0] > 0.f ? dy0 * sW.w3[c0] : 0.f;
+                const float d01 = q[1] > 0.f ? dy0 * sW.w3[c0 + 1] : 0.f;
+                const float d10 = q[2] > 0.f ? dy1 * sW.w3[c0] : 0.f;
+                const float d11 = q[3] > 0.f ? dy1 * sW.w3[c0 + 1] : 0.f;
+                tw.h2[r0 * HROW + c0] = q[0];
+                tw.h2[r0 * HROW + c0 + 1] = q[1];
+                tw.h2[r1 * HROW + c0] = q[2];
+                tw.h2[r1 * HROW + c0 + 1] = q[3];
+                tw.dh2[r0 * HROW + c0] = d00;
+                tw.dh2[r0 * HROW + c0 + 1] = d01;
+                tw.dh2[r1 * HROW + c0] = d10;
+                tw.dh2[r1 * HROW + c0 + 1] = d11;
+                *reinterpret_cast<__nv_bfloat162 *>(tw.dh2b + r0 * SH_STRIDE + c0) =
+                    __floats2bfloat162_rn(d00, d01);
+                *reinterpret_cast<__nv_bfloat162 *>(tw.dh2b + r1 * SH_STRIDE + c0) =
+                    __floats2bfloat162_rn(d10, d11);
             }
+        }
         __syncwarp();
-        // per-sample backward (row = lane)
-        const float err = valid ? tw.m.y[lane] - Z[s] : 0.f;
-        const float dy = 2.f * err * inv_n;
-        tw.dy[lane] = dy;
-        float *h2r = tw.h2 + lane * HROW, *dh2r = tw.dh2 + lane * HROW;
-        for (int j = 0; j < MLP_H; j++) dh2r[j] = h2r[j] > 0.f ? dy * sW.w3[j] : 0.f;
-        float *dh1r = tw.dh1 + lane * HROW;
-        const __nv_bfloat16 *h1r = tw.m.h1 + lane * SH_STRIDE;
-        for (int i = 0; i < MLP_H; i++) {
-            float acc = 0.f;
-            if (__bfloat162float(h1r[i]) > 0.f)
-                for (int j = 0; j < MLP_H; j++)
-                    acc = acc + dh2r[j] * __bfloat162float(sW.w2[j * SW2_STRIDE + i]);
-            dh1r[i] = acc;
+        // dH1 = (dH2 W2) (h1 > 0): A = dH2 [samples x 64], B[k = j][n = i] = W2[j][i]
+#pragma unroll 1
+        for (int mt = 0; mt < 2; mt++) {
+            float acc[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+            for (int kt = 0; kt < 4; kt++) {
+                const __nv_bfloat16 *da = tw.dh2b + (mt * 16 + g) * SH_STRIDE + kt * 16 + 2 * t;
+                const uint32_t a[4] = {ld_b32(da), ld_b32(da + 8 * SH_STRIDE), ld_b32(da + 8),
+                                       ld_b32(da + 8 * SH_STRIDE + 8)};
+#pragma unroll
+                for (int np = 0; np < 4; np++) {
+                    uint32_t b[4];
+                    ldsm_x4_trans(b, sW.w2 + (kt * 16 + lr_b) * SW2_STRIDE + np * 16 + lc_b);
+                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+                    mma_bf16_16816(acc[2 * np], a, b0);
+                    mma_bf16_16816(acc[2 * np + 1], a, b1);
+                }
+            }
+            const int r0 = mt * 16 + g, r1 = r0 + 8;
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int c0 = nt * 8 + 2 * t;
+                const __nv_bfloat16 *h1r0 = tw.m.h1 + r0 * SH_STRIDE + c0;
+                const __nv_bfloat16 *h1r1 = tw.m.h1 + r1 * SH_STRIDE + c0;
+                const float d00 = __bfloat162float(h1r0[0]) > 0.f ? acc[nt][0] : 0.f;
+                const float d01 = __bfloat162float(h1r0[1]) > 0.f ? acc[nt][1] : 0.f;
+                const float d10 = __bfloat162float(h1r1[0]) > 0.f ? acc[nt][2] : 0.f;
+                const float d11 = __bfloat162float(h1r1[1]) > 0.f ? acc[nt][3] : 0.f;
+                tw.dh1[r0 * HROW + c0] = d00;
+                tw.dh1[r0 * HROW + c0 + 1] = d01;
+                tw.dh1[r1 * HROW + c0] = d10;
+                tw.dh1[r1 * HROW + c0 + 1] = d11;
+                *reinterpret_cast<__nv_bfloat162 *>(tw.dh1b + r0 * SH_STRIDE + c0) =
+                    __floats2bfloat162_rn(d00, d01);
+                *reinterpret_cast<__nv_bfloat162 *>(tw.dh1b + r1 * SH_STRIDE + c0) =
+                    __floats2bfloat162_rn(d10, d11);
+            }
         }
         // block loss: sum over the warp, one atomic per warp into shared memory
         float e2 = err * err;
         for (int d = 16; d > 0; d >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, d);
         if (lane == 0) atomicAdd(&sG[MLP_NPARAM], e2 * inv_n);
         __syncthreads();
-        // weight gradients: every thread owns a strided subset of the parameters
-        for (int p = threadIdx.x; p < MLP_NPARAM; p += blockDim.x) {
+        // dW2 rows j = 16 wid .. 16 wid + 15 (all 64 columns) and dW1 rows
+        // i = 16 wid .. (inputs 0..31) over the block's 128 samples: k-step kk
+        // is samples 16 kk .. 16 kk + 15, rows 16 (kk & 1) .. of warp kk / 2's tiles
+        {
+            float a2[8][4], a1[4][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) a2[nt][0] = a2[nt][1] = a2[nt][2] = a2[nt][3] = 0.f;
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) a1[nt][0] = a1[nt][1] = a1[nt][2] = a1[nt][3] = 0.f;
+#pragma unroll 1
+            for (int kk = 0; kk < 2 * TRAIN_WARPS; kk++) {
+                const TrainSmemWarp &u = sWarp[kk >> 1];
+                const int sr = (kk & 1) * 16;
+                uint32_t a[4];
+                // A[m = j][k = sample] = dH2[sample][j]
+                ldsm_x4_trans(a, u.dh2b + (sr + lr_a) * SH_STRIDE + wid * 16 + lc_a);
+#pragma unroll
+                for (int np = 0; np < 4; np++) {
+                    uint32_t b[4];  // B[k = sample][n = i] = h1[sample][i]
+                    ldsm_x4_trans(b, u.m.h1 + (sr + lr_b) * SH_STRIDE + np * 16 + lc_b);
+                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+                    mma_bf16_16816(a2[2 * np], a, b0);
+                    mma_bf16_16816(a2[2 * np + 1], a, b1);
+                }
+                // A[m = i][k = sample] = dH1[sample][i]
+                ldsm_x4_trans(a, u.dh1b + (sr + lr_a) * SH_STRIDE + wid * 16 + lc_a);
+#pragma unroll
+                for (int np = 0; np < 2; np++) {
+                    uint32_t b[4];  // B[k = sample][n = input] = x[sample][input]
+                    ldsm_x4_trans(b, u.m.x + (sr + lr_b) * SX_STRIDE + np * 16 + lc_b);
+                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+                    mma_bf16_16816(a1[2 * np], a, b0);
+                    mma_bf16_16816(a1[2 * np + 1], a, b1);
+                }
+            }
+            const int j0 = wid * 16 + g, j1 = j0 + 8;
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int c0 = nt * 8 + 2 * t;
+                sG[MLP_OFF_W2 + j0 * MLP_H + c0] += a2[nt][0];
+                sG[MLP_OFF_W2 + j0 * MLP_H + c0 + 1] += a2[nt][1];
+                sG[MLP_OFF_W2 + j1 * MLP_H + c0] += a2[nt][2];
+                sG[MLP_OFF_W2 + j1 * MLP_H + c0 + 1] += a2[nt][3];
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const int f0 = nt * 8 + 2 * t;
+                if (f0 < MLP_IN) {
+                    sG[MLP_OFF_W1 + j0 * MLP_IN + f0] += a1[nt][0];
+                    sG[MLP_OFF_W1 + j1 * MLP_IN + f0] += a1[nt][2];
+                }
+                if (f0 + 1 < MLP_IN) {
+                    sG[MLP_OFF_W1 + j0 * MLP_IN + f0 + 1] += a1[nt][1];
+                    sG[MLP_OFF_W1 + j1 * MLP_IN + f0 + 1] += a1[nt][3];
+                }
+            }
+        }
+        // db1, db2, dw3, db3: FP32 sums over the 128 samples, one owner each
+        for (int q = threadIdx.x; q < 3 * MLP_H + 1; q += blockDim.x) {
             float acc = 0.f;
             for (int w = 0; w < TRAIN_WARPS; w++) {
                 const TrainSmemWarp &u = sWarp[w];
                 for (int r = 0; r < 32; r++) {
-                    float v;
-                    if (p < MLP_OFF_B1) {
-                        const int j = p / MLP_IN, f = p % MLP_IN;
-                        v = u.dh1[r * HROW + j] * __bfloat162float(u.m.x[r * SX_STRIDE + f]);
-                    } else if (p < MLP_OFF_W2) {
-                        v = u.dh1[r * HROW + (p - MLP_OFF_B1)];
-                    } else if (p < MLP_OFF_B2) {
-                        const int q = p - MLP_OFF_W2, j = q / MLP_H, i = q % MLP_H;
-                        v = u.dh2[r * HROW + j] * __bfloat162float(u.m.h1[r * SH_STRIDE + i]);
-                    } else if (p < MLP_OFF_W3) {
-                        v = u.dh2[r * HROW + (p - MLP_OFF_B2)];
-                    } else if (p < MLP_OFF_B3) {
-                        v = u.dy[r] * u.h2[r * HROW + (p - MLP_OFF_W3)];
-                    } else {
-                        v = u.dy[r];
-                    }
-                    acc = acc + v;
+                    if (q < MLP_H) acc = acc + u.dh1[r * HROW + q];
+                    else if (q < 2 * MLP_H) acc = acc + u.dh2[r * HROW + q - MLP_H];
+                    else if (q < 3 * MLP_H) acc = acc + u.dy[r] * u.h2[r * HROW + q - 2 * MLP_H];
+                    else acc = acc + u.dy[r];
                 }
             }
+            const int p = q < MLP_H ? MLP_OFF_B1 + q
+                        : q < 2 * MLP_H ? MLP_OFF_B2 + q - MLP_H
+                        : q < 3 * MLP_H ? MLP_OFF_W3 + q - 2 * MLP_H
+                                        : MLP_OFF_B3;
             sG[p] = sG[p] + acc;
         }
         __syncthreads();

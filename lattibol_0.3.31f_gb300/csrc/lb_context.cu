@@ -62,6 +62,12 @@ struct lb_ctx {
     // copies of the interior tiles' stages); 0 unknown, 1 encoded, -1 not available
     CUtensorMap tmap[2];
     int tmap_state[2] = {0, 0};
+    // lb_slab_group_step on this slab as the group's first: graph-captured
+    // batches of steps of the group (key: the group's slab list), one graph
+    // per starting (population set, face parity)
+    std::vector<lb_ctx *> grp_key;
+    cudaGraphExec_t grp_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaEvent_t ev_fork = nullptr;
 };
 
 namespace {
@@ -505,8 +511,11 @@ int lb_destroy(lb_ctx *c) {
     if (c->probe_host) cudaFreeHost(c->probe_host);
     if (c->side) cudaStreamSynchronize(c->side);
     for (int i = 0; i < 2; i++)
-        for (int j = 0; j < 2; j++)
+        for (int j = 0; j < 2; j++) {
             if (c->face[i][j]) cudaFree(c->face[i][j]);
+            if (c->grp_graph[i][j]) cudaGraphExecDestroy(c->grp_graph[i][j]);
+        }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     for (cudaEvent_t ev : {c->ev0, c->ev1, c->ev_in, c->ev_done, c->ev_pack})
         if (ev) cudaEventDestroy(ev);
     if (c->side) cudaStreamDestroy(c->side);
@@ -1172,7 +1181,7 @@ int lb_slab_create(const lb_config *global, int z0, int nz, lb_ctx **out) {
     c->slab_z0 = z0;
     c->slab_nz_global = global->nz;
     cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
-    for (cudaEvent_t *ev : {&c->ev_in, &c->ev_done, &c->ev_pack})
+    for (cudaEvent_t *ev : {&c->ev_in, &c->ev_done, &c->ev_pack, &c->ev_fork})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     const size_t fb = (size_t)5 * plane_of(c) * c->esize;
     for (int i = 0; i < 2; i++)
@@ -1240,6 +1249,110 @@ int lb_slab_unpack(lb_ctx *c, const void *from_below, const void *from_above) {
     return LB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// one step of every slab of a group, the faces moved by device copies (the
+// unpack kernel of each slab reads its neighbours' packed faces); packs
+// alternate between two buffers by step parity, so a slab's next pack never
+// overwrites a face its neighbours may still be reading
+int group_step_once(lb_ctx *const *slabs, int n, bool moments) {
+    auto bad = [&](lb_ctx *c, cudaError_t e) {
+        cuda_fail(c, "lb_slab_group_step", e);
+        abi_record_error("lb_slab_group_step", c->err.c_str());
+        return LB_ERR_CUDA;
+    };
+    for (int i = 0; i < n; i++) {
+        lb_ctx *c = slabs[i];
+        int rc = lb_slab_step(c, moments ? 1 : 0, c->face[c->parity][0], c->face[c->parity][1]);
+        if (rc != LB_OK) {
+            abi_record_error("lb_slab_group_step", c->err.c_str());
+            return rc;
+        }
+        cudaError_t e = cudaEventRecord(c->ev_pack, c->stream);
+        if (e != cudaSuccess) return bad(c, e);
+    }
+    for (int i = 0; i < n; i++) {
+        lb_ctx *c = slabs[i], *lo = slabs[(i + n - 1) % n], *hi = slabs[(i + 1) % n];
+        cudaError_t e = cudaSuccess;
+        if (lo != c) e = cudaStreamWaitEvent(c->stream, lo->ev_pack, 0);
+        if (e == cudaSuccess && hi != c && hi != lo)
+            e = cudaStreamWaitEvent(c->stream, hi->ev_pack, 0);
+        if (e != cudaSuccess) return bad(c, e);
+        int rc = lb_slab_unpack(c, lo->face[lo->parity][1], hi->face[hi->parity][0]);
+        if (rc != LB_OK) {
+            abi_record_error("lb_slab_group_step", c->err.c_str());
+            return rc;
+        }
+    }
+    for (int i = 0; i < n; i++) slabs[i]->parity ^= 1;
+    return LB_OK;
+}
+
+// slabs[1..] wait for the work queued so far on slabs[0]'s stream (or the
+// reverse with `join`): the group's streams fork from and join into it
+cudaError_t group_fork(lb_ctx *const *slabs, int n) {
+    lb_ctx *c0 = slabs[0];
+    cudaError_t e = cudaEventRecord(c0->ev_fork, c0->stream);
+    for (int i = 1; i < n && e == cudaSuccess; i++)
+        e = cudaStreamWaitEvent(slabs[i]->stream, c0->ev_fork, 0);
+    return e;
+}
+cudaError_t group_join(lb_ctx *const *slabs, int n) {
+    lb_ctx *c0 = slabs[0];
+    cudaError_t e = cudaSuccess;
+    for (int i = 1; i < n && e == cudaSuccess; i++) {
+        e = cudaEventRecord(slabs[i]->ev_fork, slabs[i]->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c0->stream, slabs[i]->ev_fork, 0);
+    }
+    return e;
+}
+
+// G steps of the group (G even: every slab returns to its population set and
+// face parity) captured once as one graph on slabs[0]'s stream
+int group_graph(lb_ctx *const *slabs, int n, int G, cudaGraphExec_t *out) {
+    lb_ctx *c0 = slabs[0];
+    const std::vector<lb_ctx *> key(slabs, slabs + n);
+    if (c0->grp_key != key) {
+        for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++)
+                if (c0->grp_graph[i][j]) {
+                    cudaGraphExecDestroy(c0->grp_graph[i][j]);
+                    c0->grp_graph[i][j] = nullptr;
+                }
+        c0->grp_key = key;
+    }
+    cudaGraphExec_t &slot = c0->grp_graph[c0->cur][c0->parity];
+    if (slot) { *out = slot; return LB_OK; }
+    std::vector<int64_t> before(n);
+    for (int i = 0; i < n; i++) before[i] = slabs[i]->launches;
+    cudaError_t e = cudaStreamBeginCapture(c0->stream, cudaStreamCaptureModeThreadLocal);
+    int rc = LB_OK;
+    if (e == cudaSuccess) e = group_fork(slabs, n);
+    for (int t = 0; t < G && e == cudaSuccess && rc == LB_OK; t++)
+        rc = group_step_once(slabs, n, false);
+    if (e == cudaSuccess && rc == LB_OK) e = group_join(slabs, n);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(c0->stream, &graph);
+    for (int i = 0; i < n; i++) slabs[i]->launches = before[i];  // capture launches nothing
+    if (rc != LB_OK) return rc;
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&slot, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        slot = nullptr;
+        abi_record_error("lb_slab_group_step (graph capture)", cudaGetErrorString(e));
+        return LB_ERR_CUDA;
+    }
+    *out = slot;
+    return LB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int lb_slab_group_step(lb_ctx *const *slabs, int n, int nsteps) {
     if (!slabs || n < 1 || nsteps < 0) return LB_ERR_ARG;
     int dev = -1;
@@ -1256,41 +1369,38 @@ int lb_slab_group_step(lb_ctx *const *slabs, int n, int nsteps) {
         }
     }
     if (cudaGetDevice(&dev) != cudaSuccess) return LB_ERR_CUDA;
-    auto bad = [&](lb_ctx *c, cudaError_t e) {
-        cuda_fail(c, "lb_slab_group_step", e);
-        abi_record_error("lb_slab_group_step", c->err.c_str());
-        return LB_ERR_CUDA;
-    };
-    for (int t = 0; t < nsteps; t++) {
-        const bool last = t == nsteps - 1;
-        for (int i = 0; i < n; i++) {
-            lb_ctx *c = slabs[i];
-            int rc = lb_slab_step(c, last ? 1 : 0, c->face[c->parity][0], c->face[c->parity][1]);
-            if (rc != LB_OK) {
-                abi_record_error("lb_slab_group_step", c->err.c_str());
-                return rc;
-            }
-            cudaError_t e = cudaEventRecord(c->ev_pack, c->stream);
-            if (e != cudaSuccess) return bad(c, e);
-        }
-        for (int i = 0; i < n; i++) {
-            lb_ctx *c = slabs[i], *lo = slabs[(i + n - 1) % n], *hi = slabs[(i + 1) % n];
-            cudaError_t e = cudaSuccess;
-            if (lo != c) e = cudaStreamWaitEvent(c->stream, lo->ev_pack, 0);
-            if (e == cudaSuccess && hi != c && hi != lo)
-                e = cudaStreamWaitEvent(c->stream, hi->ev_pack, 0);
-            if (e != cudaSuccess) return bad(c, e);
-            int rc = lb_slab_unpack(c, lo->face[lo->parity][1], hi->face[hi->parity][0]);
-            if (rc != LB_OK) {
-                abi_record_error("lb_slab_group_step", c->err.c_str());
-                return rc;
-            }
-        }
-        // the next step packs into the other buffers: a slab's next pack then
-        // never overwrites a face its neighbours may still be reading
-        for (int i = 0; i < n; i++) slabs[i]->parity ^= 1;
+    for (int i = 0; i < n; i++) {  // a caller's earlier steps may leave interior planes open
+        if (slab_join(slabs[i]) != cudaSuccess) return LB_ERR_CUDA;
     }
-    return LB_OK;
+    // all but the last step in graphs of G steps; the last writes the moments
+    const int G = std::max(2, slabs[0]->cfg.graph_steps & ~1);
+    int rest = nsteps - 1;
+    if (rest >= G) {
+        if (group_join(slabs, n) != cudaSuccess) return LB_ERR_CUDA;
+        while (rest >= G) {
+            cudaGraphExec_t gr;
+            int rc = group_graph(slabs, n, G, &gr);
+            if (rc != LB_OK) return rc;
+            const cudaError_t e = cudaGraphLaunch(gr, slabs[0]->stream);
+            if (e != cudaSuccess) {
+                abi_record_error("lb_slab_group_step", cudaGetErrorString(e));
+                return LB_ERR_CUDA;
+            }
+            for (int i = 0; i < n; i++) {
+                lb_ctx *c = slabs[i];
+                c->launches += (int64_t)G * (c->slab_nz > 2 ? 4 : 3);
+                c->steps += G;
+                if (G & 1) c->cur = 1 - c->cur;  // (G is even: every slab returns)
+            }
+            rest -= G;
+        }
+        if (group_fork(slabs, n) != cudaSuccess) return LB_ERR_CUDA;
+    }
+    for (; rest > 0; rest--) {
+        const int rc = group_step_once(slabs, n, false);
+        if (rc != LB_OK) return rc;
+    }
+    return nsteps > 0 ? group_step_once(slabs, n, true) : LB_OK;
 }
 
 int lb_slab_group_time(lb_ctx *const *slabs, int n, int nsteps, float *ms) {

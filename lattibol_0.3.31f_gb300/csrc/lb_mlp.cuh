@@ -69,6 +69,18 @@ __device__ __forceinline__ uint32_t ld_b32(const __nv_bfloat16 *p) {
     return *reinterpret_cast<const uint32_t *>(p);
 }
 
+// Four 8x8 bf16 matrices from shared memory, each transposed on the way
+// (ldmatrix .trans): lane l gives the address of row l % 8 of matrix l / 8
+// (16 contiguous bytes, 16-byte aligned); register q receives matrix q in the
+// fragment layout of an mma operand whose rows are the stored columns.
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const __nv_bfloat16 *row) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a)
+                 : "memory");
+}
+
 // all threads of the block: stage the network in shared memory
 __device__ __forceinline__ void mlp_load_weights(MlpSmemWeights &s, const MlpDev &m) {
     for (int i = threadIdx.x + blockDim.x * threadIdx.y; i < MLP_H * MLP_IN_PAD;

@@ -52,7 +52,10 @@ def forward(p, X):
 
 def grad(p, X, Z):
     """Gradient of mean((y - z)^2) over the rows, with the rounding treated as
-    the identity in the backward pass (as the GPU backward does)."""
+    the identity in the backward pass except where the GPU backward rounds:
+    its contractions run on the tensor cores, so dH2 enters dH1 = dH2 W2 and
+    dW2 = dH2^T H1, and dH1 enters dW1 = dH1^T X, as bfloat16 (the bias
+    gradients sum the unrounded values)."""
     W1, b1, W2, b2, w3, b3 = unpack(p)
     f = forward(p, X)
     n = len(X)
@@ -61,10 +64,11 @@ def grad(p, X, Z):
     g[OFF_W3:OFF_B3] = f["h2"].T @ dy
     g[OFF_B3] = dy.sum()
     dh2 = (dy[:, None] * w3[None, :]) * (f["h2"] > 0)
-    g[OFF_W2:OFF_B2] = (dh2.T @ f["h1"]).reshape(-1)
+    dh2b = bf16(dh2).astype(np.float64)
+    g[OFF_W2:OFF_B2] = (dh2b.T @ f["h1"]).reshape(-1)
     g[OFF_B2:OFF_W3] = dh2.sum(0)
-    dh1 = (dh2 @ f["W2b"]) * (f["h1"] > 0)
-    g[OFF_W1:OFF_B1] = (dh1.T @ f["xb"]).reshape(-1)
+    dh1 = (dh2b @ f["W2b"]) * (f["h1"] > 0)
+    g[OFF_W1:OFF_B1] = (bf16(dh1).astype(np.float64).T @ f["xb"]).reshape(-1)
     g[OFF_B1:OFF_W2] = dh1.sum(0)
     loss = float(np.mean((f["y"] - Z) ** 2))
     return g, loss
