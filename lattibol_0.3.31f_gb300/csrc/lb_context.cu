@@ -1325,8 +1325,11 @@ int group_graph(lb_ctx *const *slabs, int n, int G, cudaGraphExec_t *out) {
     }
     cudaGraphExec_t &slot = c0->grp_graph[c0->cur][c0->parity];
     if (slot) { *out = slot; return LB_OK; }
-    std::vector<int64_t> before(n);
-    for (int i = 0; i < n; i++) before[i] = slabs[i]->launches;
+    std::vector<int64_t> before(n), steps_before(n);
+    for (int i = 0; i < n; i++) {
+        before[i] = slabs[i]->launches;
+        steps_before[i] = slabs[i]->steps;
+    }
     cudaError_t e = cudaStreamBeginCapture(c0->stream, cudaStreamCaptureModeThreadLocal);
     int rc = LB_OK;
     if (e == cudaSuccess) e = group_fork(slabs, n);
@@ -1335,7 +1338,10 @@ int group_graph(lb_ctx *const *slabs, int n, int G, cudaGraphExec_t *out) {
     if (e == cudaSuccess && rc == LB_OK) e = group_join(slabs, n);
     cudaGraph_t graph = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(c0->stream, &graph);
-    for (int i = 0; i < n; i++) slabs[i]->launches = before[i];  // capture launches nothing
+    for (int i = 0; i < n; i++) {  // capture launches nothing and advances no step
+        slabs[i]->launches = before[i];
+        slabs[i]->steps = steps_before[i];
+    }
     if (rc != LB_OK) return rc;
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&slot, graph, 0);
@@ -1389,8 +1395,7 @@ int lb_slab_group_step(lb_ctx *const *slabs, int n, int nsteps) {
             for (int i = 0; i < n; i++) {
                 lb_ctx *c = slabs[i];
                 c->launches += (int64_t)G * (c->slab_nz > 2 ? 4 : 3);
-                c->steps += G;
-                if (G & 1) c->cur = 1 - c->cur;  // (G is even: every slab returns)
+                c->steps += G;  // G is even: every slab is back on its set and parity
             }
             rest -= G;
         }

@@ -316,31 +316,6 @@ __global__ void d2q9_equilibrium_kernel(Pop<9> p, const float *rho, const float 
 // Pulls bypass L1 (ld.global.cg): L1 does not see the other SMs' stores.  The
 // per-node arithmetic is d2q9_fused_kernel's, so results are the same bits.
 // ---------------------------------------------------------------------------
-constexpr int PERSIST_SPIN_LIMIT = 1 << 22;
-
-__device__ __forceinline__ void st_release_gpu(int *p, int v) {
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// true once *flag >= target; false when this wait gave up (it then raises
-// *err) or another block already has
-__device__ bool wait_band(const int *flag, int target, int *err, int limit = PERSIST_SPIN_LIMIT) {
-    for (int i = 0; i < limit; i++) {
-        if (ld_acquire_gpu(flag) >= target) return true;
-        if ((i & 63) == 63) {
-            if (ld_acquire_gpu(err) != 0) return false;
-            __nanosleep(100);
-        }
-    }
-    atomicExch(err, 1);
-    return false;
-}
-
 template <int MODE>
 __device__ __forceinline__ void d2q9_node_l2(const D2Args &a, int par, int x, int y, bool mom) {
     // par = 0: a.src -> a.dst; par = 1: the other way

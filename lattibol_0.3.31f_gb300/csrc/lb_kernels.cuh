@@ -86,6 +86,35 @@ struct D2Args {
     int probe_o;
 };
 
+// ---- waits between blocks of one persistent launch (all blocks resident):
+// release/acquire at GPU scope, and a bounded spin that raises an error word
+// instead of waiting forever
+constexpr int PERSIST_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// true once *flag >= target; false when this wait gave up (it then raises
+// *err) or another block already has
+__device__ __forceinline__ bool wait_band(const int *flag, int target, int *err,
+                                          int limit = PERSIST_SPIN_LIMIT) {
+    for (int i = 0; i < limit; i++) {
+        if (ld_acquire_gpu(flag) >= target) return true;
+        if ((i & 63) == 63) {
+            if (ld_acquire_gpu(err) != 0) return false;
+            __nanosleep(100);
+        }
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
 // D3Q19
 cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, cudaStream_t s);
 // native mode with storage kind (0 f32, 1 f16, 2 bf16) and optional Shan-Chen

@@ -53,11 +53,12 @@ class Slab(Lattice):
     the ghost plane below, the own planes, the ghost plane above."""
 
     def __init__(self, nx, ny, nz_global, z0, nz, tau_inv=1.0, force=(0, 0, 0),
-                 wall_u=(0, 0, 0), storage=abi.LB_STORE_F32, rho_ref=0.0):
+                 wall_u=(0, 0, 0), storage=abi.LB_STORE_F32, rho_ref=0.0, graph_steps=64):
         L = _lib()
         cfg = abi.lb_config()
         L.lb_config_default(ctypes.byref(cfg), 19, nx, ny, nz_global)
         cfg.mode, cfg.tau_inv, cfg.storage, cfg.rho_ref = abi.LB_MODE_NATIVE, tau_inv, storage, rho_ref
+        cfg.graph_steps = graph_steps  # lb_slab_group_step: steps per captured graph
         for i in range(3):
             cfg.force[i], cfg.wall_u[i] = force[i], wall_u[i]
         h = ctypes.c_void_p()

@@ -43,12 +43,13 @@ def whole(pkg, fl, f, steps, storage=0):
     return out
 
 
-def make_slabs(pkg, fl, f, bounds, storage=0):
+def make_slabs(pkg, fl, f, bounds, storage=0, graph_steps=64):
     S = pkg.slab
     P = W * H
     slabs = []
     for z0, nz in bounds:
-        s = S.Slab(W, H, D, z0, nz, storage=storage, rho_ref=1.0 if storage else 0.0, **PHYS)
+        s = S.Slab(W, H, D, z0, nz, storage=storage, rho_ref=1.0 if storage else 0.0,
+                   graph_steps=graph_steps, **PHYS)
         planes = s.planes()
         s.set_flags(np.ascontiguousarray(fl.reshape(D, P)[planes].reshape(-1)))
         s.set_populations(np.ascontiguousarray(f.reshape(19, D, P)[:, planes].reshape(19, -1)))
@@ -89,6 +90,30 @@ def test_slab_group_bit_exact(pkg, oracle, bounds):
     reds = np.array([s.reduce() for s in slabs])
     np.testing.assert_allclose(reds[:, :5].sum(axis=0), red_ref[:5], rtol=1e-12, atol=1e-15)
     assert reds[:, 5].max() == red_ref[5] and reds[:, 6].sum() == red_ref[6]
+    for s in slabs:
+        s.close()
+
+
+@pytest.mark.parametrize("bounds", [[(0, 18)], [(0, 7), (7, 4), (11, 7)]], ids=["one", "three"])
+def test_slab_group_graphs(pkg, oracle, bounds):
+    """Batches replayed from captured graphs (4 steps each, on every slab's
+    two streams), then eager steps: the same bits as one context, and the
+    step counts and moments of the last step follow."""
+    fl, f = setup(pkg, oracle, seed=9)
+    steps = 23
+    f_ref, mom_ref, _ = whole(pkg, fl, f, steps)
+    slabs = make_slabs(pkg, fl, f, bounds, graph_steps=4)
+    grp = pkg.slab.SlabGroup(slabs)
+    grp.step(13)   # three graphs of 4, one eager step
+    grp.step(10)   # the graphs again (same set and parity), then one eager step
+    grp.synchronize()
+    got, mom = gather(slabs)
+    assert np.array_equal(got.view(np.uint32), f_ref.view(np.uint32))
+    for a, b in zip(mom, mom_ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert all(s.steps_done() == steps for s in slabs)
+    ms = grp.time_steps(9)
+    assert ms > 0 and all(s.steps_done() == steps + 9 for s in slabs)
     for s in slabs:
         s.close()
 
