@@ -187,6 +187,7 @@ cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s);
 // the moments of the last one.  tblock_steps is 0 for an unknown variant.
 int tblock_steps(int variant);
 cudaError_t launch_d2q9_tblock(const D2Args &a, int variant, bool mom, cudaStream_t s);
+
 cudaError_t launch_d2q9_stream_swap(const Pop<9> &p, const uint8_t *sb, int W, int H,
                                     cudaStream_t s);
 cudaError_t launch_d2q9_collide(const D2Args &a, bool plot, cudaStream_t s);
