@@ -169,10 +169,6 @@ typedef enum {
 /* launch tuning (lb_config.tuning); results do not depend on it */
 #define LB_TUNE_DEFAULT 0      /* the library's measured choice */
 #define LB_TUNE_EXPLICIT 0x100 /* use exactly the bits below */
-#define LB_TUNE_SC_SINGLE_PASS 0x002 /* D3Q19 Shan-Chen: the single-pass z-marching
-                                        kernel (psi halo in shared memory) instead of
-                                        the separate psi pass; same results, measured
-                                        slower (24.8 vs 26.3 GLUPS FP32 at 256^3) */
 #define LB_TUNE_PERSISTENT 0x004 /* D2Q9 without Shan-Chen: lb_step runs all its steps
                                     in one cooperative launch whose blocks own row
                                     bands and wait (bounded) only for their two

@@ -304,10 +304,6 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
                                          c->tmap_state[from] > 0 ? &c->tmap[from] : nullptr,
                                          c->stream);
         }
-        if (sc && (c->tune & LB_TUNE_SC_SINGLE_PASS) && sc_march_chunk(g.nx, g.ny, g.nz)) {
-            c->launches += 1;
-            return launch_d3q19_sc_march(a, g.storage, moments, c->stream);
-        }
         c->launches += sc ? 2 : 1;
         return launch_d3q19_native(a, g.storage, moments, sc, c->stream);
     }
@@ -355,9 +351,6 @@ int graph_for(lb_ctx *c, int from, cudaGraphExec_t *out) {
 int launches_per_step(const lb_ctx *c) {
     if (!sc_on(c)) return 1;
     if (sc_stage_on(c)) return 1;
-    if (c->Q == 19 && c->cfg.mode == LB_MODE_NATIVE && (c->tune & LB_TUNE_SC_SINGLE_PASS) &&
-        sc_march_chunk(c->cfg.nx, c->cfg.ny, c->cfg.nz))
-        return 1;
     return 2;
 }
 

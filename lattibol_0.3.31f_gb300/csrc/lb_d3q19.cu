@@ -134,150 +134,6 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_density_kernel(const D3Args a)
     a.psi[o] = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
 }
 
-// ---------------------------------------------------------------------------
-// Single-pass Shan-Chen step.  A block owns a SC_TX x SC_TY column tile and
-// marches through a chunk of planes.  For plane z + 1 it pulls the
-// populations of its 256 nodes (kept in shared memory, each thread's own
-// column of a plane buffer) and of the 84-node ring around them and writes
-// their psi into one of four plane slots; after one barrier it relaxes plane
-// z from the populations it kept one plane earlier and the psi stencil of
-// planes z - 1, z, z + 1.  DRAM sees each population once per step and psi
-// never leaves the SM.  Four psi slots make one barrier per plane enough: a
-// warp writing the slot of plane z + 2 has passed the barrier of plane z + 1,
-// which every warp reaches only after relaxing plane z - 1, the last reader of
-// that slot; the population buffers are private to their thread.  Keeping
-// the populations in shared memory rather than registers holds the kernel at
-// 64 registers (4 blocks per SM).  The arithmetic is the two-pass path's
-// (same pulls, rho sum, stencil order), so both produce the same bits.
-// ---------------------------------------------------------------------------
-constexpr int SC_TX = 32, SC_TY = 8, SC_HX = SC_TX + 2, SC_HY = SC_TY + 2;
-constexpr int SC_THREADS = SC_TX * SC_TY;            // 256
-constexpr int SC_HALO = SC_HX * SC_HY - SC_THREADS;  // 84
-
-template <typename S>
-__device__ __forceinline__ float sc_psi_of_node(const D3Args &a, int x, int y, int zz) {
-    const int o = x + a.W * (y + a.H * zz);
-    const uint8_t fl = a.flags[o];
-    if (fl & CELL_WALL) return 0.f;
-    const Nbr3 n(x, y, zz, a.W, a.H, a.D);
-    float g[19];
-    pull_native<S>(a, o, n, fl, g);
-    const float rho = StepArith<S>::rho(g, a);
-    return a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
-}
-
-template <typename S, bool MOM>
-__global__ void __launch_bounds__(SC_THREADS, 4) d3q19_sc_march_kernel(const D3Args a, int zc) {
-    __shared__ float sp[4][SC_HY][SC_HX];
-    __shared__ float sg[2][19][SC_THREADS];  // pulled populations of planes z, z + 1
-    const int tid = threadIdx.x, tx = tid % SC_TX, ty = tid / SC_TX;
-    const int x0 = blockIdx.x * SC_TX, y0 = blockIdx.y * SC_TY, z0 = blockIdx.z * zc;
-    const int x = x0 + tx, y = y0 + ty;
-    // the halo node this thread also handles (tid < 84): two rows of 34, then
-    // the two side columns of 8
-    int hx = 0, hy = 0;
-    if (tid < 2 * SC_HX) {
-        hx = tid % SC_HX - 1;
-        hy = tid < SC_HX ? -1 : SC_TY;
-    } else if (tid < SC_HALO) {
-        hx = (tid - 2 * SC_HX) < SC_TY ? -1 : SC_TX;
-        hy = (tid - 2 * SC_HX) % SC_TY;
-    }
-    const int hxg = (x0 + hx + a.W) % a.W, hyg = (y0 + hy + a.H) % a.H;
-    // psi of plane zl (own node and ring node) into its slot; the own node's
-    // pulled populations into buffer zl & 1
-    auto psi_plane = [&](int zl) {
-        const int zz = (zl % a.D + a.D) % a.D;
-        const int s = (zl + 4) & 3;
-        const int o = x + a.W * (y + a.H * zz);
-        const uint8_t fl = a.flags[o];
-        float psi = 0.f;
-        if (!(fl & CELL_WALL)) {
-            float g[19];
-            const Nbr3 n(x, y, zz, a.W, a.H, a.D);
-            pull_native<S>(a, o, n, fl, g);
-            const float rho = StepArith<S>::rho(g, a);
-            psi = a.psi_form == 0 ? psi_ref(rho) : psi_exp1(rho);
-#pragma unroll
-            for (int k = 0; k < 19; k++) sg[zl & 1][k][tid] = g[k];
-        }
-        sp[s][ty + 1][tx + 1] = psi;
-        if (tid < SC_HALO) sp[s][hy + 1][hx + 1] = sc_psi_of_node<S>(a, hxg, hyg, zz);
-    };
-
-    psi_plane(z0 - 1);
-    psi_plane(z0);
-    for (int z = z0; z < z0 + zc; z++) {
-        psi_plane(z + 1);
-        __syncthreads();
-        const int o = x + a.W * (y + a.H * z);
-        const uint8_t fl = a.flags[o];
-        if (!(fl & CELL_WALL)) {
-            float g[19];
-#pragma unroll
-            for (int k = 0; k < 19; k++) g[k] = sg[z & 1][k][tid];
-            float rho, ux, uy, uz;
-            StepArith<S>::moments(g, a, rho, ux, uy, uz);
-            if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
-            if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
-            const float inv_rt = 1.f / (rho * a.tau_inv);
-            float ex = ux, ey = uy, ez = uz;
-            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
-            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
-            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
-            float ps[19];
-#pragma unroll
-            for (int k = 0; k < 19; k++)
-                ps[k] = sp[(z + d3_cz(k) + 4) & 3][ty + 1 + d3_cy(k)][tx + 1 + d3_cx(k)];
-            float IFx, IFy, IFz;
-            d3q19_sc_sum_native(ps, a.w1, a.w7, IFx, IFy, IFz);
-            const float c = (-a.G * ps[0]) * inv_rt;
-            ex = __fmaf_rn(c, IFx, ex);
-            ey = __fmaf_rn(c, IFy, ey);
-            ez = __fmaf_rn(c, IFz, ez);
-            StepArith<S>::bgk(g, ex, ey, ez, rho, a, a.tau_inv);
-            S *const *dst = reinterpret_cast<S *const *>(a.dst.f);
-#pragma unroll
-            for (int k = 0; k < 19; k++) Store<S>::store_dev(dst[k] + o, g[k]);
-        } else {
-            if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
-            if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-}
-
-// z-chunk of the marching kernel for a lattice, 0 if the shape does not tile:
-// the longest march that still gives at least 1216 blocks (two waves of 4
-// blocks on 152 SMs), else the shortest
-int sc_march_chunk(int W, int H, int D) {
-    if (W % SC_TX || H % SC_TY) return 0;
-    int pick = 0;
-    for (int zc : {32, 16, 8}) {
-        if (D % zc) continue;
-        pick = zc;
-        if ((long)(W / SC_TX) * (H / SC_TY) * (D / zc) >= 1216) return zc;
-    }
-    return pick;
-}
-
-template <typename S>
-static cudaError_t sc_march_launch(const D3Args &a, bool mom, int zc, cudaStream_t s) {
-    const dim3 g(a.W / SC_TX, a.H / SC_TY, a.D / zc);
-    if (mom) d3q19_sc_march_kernel<S, true><<<g, SC_THREADS, 0, s>>>(a, zc);
-    else d3q19_sc_march_kernel<S, false><<<g, SC_THREADS, 0, s>>>(a, zc);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaStream_t s) {
-    const int zc = sc_march_chunk(a.W, a.H, a.D);
-    if (!zc) return cudaErrorInvalidValue;
-    switch (storage) {
-    case 0: return sc_march_launch<float>(a, mom, zc, s);
-    case 1: return sc_march_launch<__half>(a, mom, zc, s);
-    case 2: return sc_march_launch<__nv_bfloat16>(a, mom, zc, s);
-    }
-    return cudaErrorInvalidValue;
-}
 
 // ---------------------------------------------------------------------------
 // Reference-exact standalone streaming, src/streaming.cu:84-163: in-place

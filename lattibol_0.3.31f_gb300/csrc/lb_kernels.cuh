@@ -128,10 +128,6 @@ cudaError_t launch_d3q19_native_planes(const D3Args &a, int storage, bool mom, i
 // calling one can reach); 16-byte accesses when every pointer and `bytes` allow
 cudaError_t launch_plane_copy(const void *const *src, void *const *dst, int n, long bytes,
                               cudaStream_t s);
-// single-pass Shan-Chen step (psi halo in shared memory, z-marching tiles);
-// usable when sc_march_chunk(W, H, D) != 0
-int sc_march_chunk(int W, int H, int D);
-cudaError_t launch_d3q19_sc_march(const D3Args &a, int storage, bool mom, cudaStream_t s);
 // single-pass Shan-Chen step whose populations arrive by bulk asynchronous
 // copies (lb_sc_stage.cu); lattices without wall nodes for which
 // sc_stage_chunk(W, H, D) != 0.  A block that gives up waiting for its copies
@@ -187,7 +183,6 @@ cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s);
 // the moments of the last one.  tblock_steps is 0 for an unknown variant.
 int tblock_steps(int variant);
 cudaError_t launch_d2q9_tblock(const D2Args &a, int variant, bool mom, cudaStream_t s);
-
 cudaError_t launch_d2q9_stream_swap(const Pop<9> &p, const uint8_t *sb, int W, int H,
                                     cudaStream_t s);
 cudaError_t launch_d2q9_collide(const D2Args &a, bool plot, cudaStream_t s);

@@ -207,3 +207,28 @@ def test_slab_refuses_what_it_cannot_do(pkg):
     s.close()
     with pytest.raises(pkg.LBError):
         pkg.slab.Slab(W, H, D, 10, 9)  # past the global lattice
+
+
+def test_slab_rank_torch_transport_single_rank(pkg, oracle):
+    """The multi-process driver (SlabRank: faces in torch CUDA tensors, moved
+    on the slab's own stream wrapped as a torch ExternalStream) with one rank,
+    whose slab is its own z-neighbour: the exchange is then a local tensor
+    copy, and everything else -- the library stream seen by torch, torch
+    device buffers handed to lb_slab_step / lb_slab_unpack -- is the path the
+    NCCL ranks take."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    fl, f = setup(pkg, oracle, seed=12)
+    steps = 7
+    f_ref, mom_ref, _ = whole(pkg, fl, f, steps)
+    (s,) = make_slabs(pkg, fl, f, [(0, D)])
+    S = pkg.slab
+    sr = S.SlabRank(s, S.SlabExchange(None, 0, 1))
+    sr.refresh_ghosts()
+    sr.step(steps)
+    s.synchronize()
+    got, mom = gather([s])
+    assert np.array_equal(got.view(np.uint32), f_ref.view(np.uint32))
+    assert np.array_equal(mom[0].view(np.uint32), mom_ref[0].view(np.uint32))
+    s.close()

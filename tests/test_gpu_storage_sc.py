@@ -5,8 +5,8 @@
   the deviation arithmetic, narrowed and widened on every store, exactly like
   the kernels' loads and stores).
 * Shan-Chen (psi = 1 - exp(-rho), exp evaluated by the library's own float
-  function on both sides) is bit-exact too, through both the single-pass
-  z-marching kernel and the separate psi pass.
+  function on both sides) is bit-exact too, through the psi pass and the
+  fused step (lattices with walls; the staged step has its own tests).
 * The spinodal error study reports rho L2 error and mass drift of the FP32,
   FP16 and BF16 storage forms against the FP64 oracle (printed; bounds
   asserted).
@@ -235,13 +235,12 @@ def test_channel_storage_error_vs_fp64(pkg, oracle):
         assert report[name]["u_err"] < bound, (name, report[name])
 
 
-@pytest.mark.parametrize("tuning", [0x102, 0x100], ids=["single_pass", "two_pass"])
+@pytest.mark.parametrize("tuning", [0x100, 0], ids=["explicit", "default"])
 @pytest.mark.parametrize("storage", [0, 2], ids=["f32", "bf16"])
 def test_shan_chen_paths_with_walls_vs_oracle(pkg, oracle, tuning, storage):
-    """Both Shan-Chen paths (single-pass z-marching with the psi halo in
-    shared memory, and the separate psi pass) on a 64x16x64 box with walls,
-    a moving lid and a body force, over several z chunks: bit-exact against
-    the oracle."""
+    """The Shan-Chen step on a lattice with walls (the psi pass and the fused
+    step) on a 64x16x64 box with walls, a moving lid and a body force:
+    bit-exact against the oracle."""
     W, H, D = 64, 16, 64
     N = W * H * D
     fl = np.zeros((D, H, W), np.uint8)
