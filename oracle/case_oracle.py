@@ -15,7 +15,7 @@ A CPU restatement, in numpy, of the reference's host-side case handling:
 * the VTK text of reference src/output.cpp:52-155 (saveParVTK, saveVTK).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may use this
-module, and only as the checker.
+module, and only to verify results against.
 """
 import math
 import re

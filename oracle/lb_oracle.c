@@ -1,7 +1,8 @@
 /*
  * lb_oracle.c -- CPU oracle for the lattice Boltzmann hot path (TEST
  * INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the CPU
- * baseline leg of bench.py as the checker, never by the GPU library).
+ * baseline leg of bench.py to verify results against or to time the
+ * reference's loop, never by the GPU library).
  *
  * Build: oracle/Makefile (gcc -O2 -fopenmp -ffp-contract=off).  FP
  * contraction must stay off so that the float instantiation performs the

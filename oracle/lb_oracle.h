@@ -4,7 +4,8 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the per-step
  * update of lattibol (streaming + collision + Shan-Chen force step + border
  * pack/unpack + cursor probe).  Only the tests, the smoke check and the CPU
- * baseline leg of the benchmark load it, and only as the checker.  The GPU
+ * baseline leg of the benchmark load it, only to verify results against or to
+ * time the reference's loop.  The GPU
  * library never links against it.
  *
  * Every routine exists twice: *_f32 computes in float with the exact

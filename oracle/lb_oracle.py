@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Loaded by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` as the checker; the GPU library never imports it.  The oracle is
+``bench.py`` to verify results against; the GPU library never imports it.  The oracle is
 a C restatement of lattibol's per-step update (see lb_oracle.h); ``build()``
 compiles it with the recipe in oracle/Makefile.
 

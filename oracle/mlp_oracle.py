@@ -4,7 +4,7 @@ The closure network 19 -> 64 -> 64 -> 1 (ReLU), its mean-squared-error
 gradient, the Favre box filter of a fine lattice and the features / targets
 built from the filtered fields -- computed in float64 with the GPU kernels'
 rounding points (inputs, W1, W2 and the first hidden layer rounded to
-bfloat16).  Used only by the tests as the checker of lb_closure.cu.
+bfloat16).  Used only by the tests, to verify lb_closure.cu against.
 """
 import numpy as np
 

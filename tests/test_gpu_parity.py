@@ -192,7 +192,7 @@ def _channel_flags(W, H, D, sphere=None, lid=False):
 
 @pytest.mark.parametrize("tuning", [0x100, 0x101], ids=["forward", "alternating"])
 def test_context_native_d3q19_vs_oracle(pkg, oracle, tuning):
-    """cfg2's physics on a small box: x-periodic channel, half-way bounce-back
+    """The channel's physics on a small box: x-periodic channel, half-way bounce-back
     walls in y/z, a sphere, body force, a moving wall, 40 steps, bit-exact
     (with and without the alternating sweep order)."""
     W, H, D = 64, 24, 20
@@ -259,7 +259,7 @@ def test_context_reference_d3q19_vs_oracle(pkg, oracle):
 
 
 def test_context_lid_cavity_d2q9_vs_oracle(pkg, oracle):
-    """cfg1's physics on 64x64: closed box, top row a moving lid."""
+    """The lid-driven cavity's physics on 64x64: closed box, top row a moving lid."""
     W = H = 64
     N = W * H
     fl = np.zeros((H, W), np.uint8)
