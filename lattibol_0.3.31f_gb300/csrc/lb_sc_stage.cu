@@ -15,11 +15,13 @@
 // TMA tensor copies (cp.async.bulk.tensor.4d over the populations' own
 // arrays, one tensor map of dims (W, H, D, population)) issued by one thread
 // and completed on the slot's mbarrier by transaction count: the other 255
-// threads issue no copy instructions at all.  TMA does not wrap, so the edge
-// blocks (periodic wrap in x or y) copy the same layout in 16-byte cp.async
-// chunks instead (each warp instruction moves 512 contiguous bytes; the wrap
-// is folded into each thread's chunk addresses, formed once per block) and
-// report on the mbarrier when their copies have landed.  Stages are issued two
+// threads issue no copy instructions at all.  (The 19 boxes issued by one
+// warp, a lane each, measured slower: 38.0 against 41.9 GLUPS.)  TMA does
+// not wrap, so the edge blocks (periodic wrap in x or y) copy the same layout
+// in 16-byte cp.async chunks instead (each warp instruction moves 512
+// contiguous bytes; the wrap is folded into each thread's chunk addresses,
+// formed once per block) and report on the mbarrier when their copies have
+// landed.  Stages are issued two
 // (FP32) or three (16-bit) steps ahead of their use, so DRAM latency is
 // covered by copies in flight rather than by warps waiting on loads, and no
 // global address is formed per population and node.
@@ -38,17 +40,17 @@
 // widened the same way; rho, the stencil sum and the relaxation are the same
 // device functions in the same order (StepArith<S>: the native FP32 forms or,
 // in 16-bit storage, their deviation forms; d3q19_sc_sum_native), so the
-// result is bit-identical to
-// the density pass + fused step.
+// result is bit-identical to the density pass + fused step.
 //
 // Every mbarrier wait is bounded (wait_limit polls of about a microsecond for
 // a stage; ST_WAIT in the library's launches); a block that gives up raises
 // the device error word, waits (bounded by ST_WAIT) for the stages it still
 // has in flight, drains its threads' own copies (cp.async.wait_all) and
-// returns.  sc_stage_wait_selftest makes the first wait run
-// out (wait_limit 0) to exercise that path.  (A first form copied each stage row with one cp.async.bulk per
-// population and row, 228 copies per stage: 20.9 GLUPS for FP32 and 16-bit
-// alike at 256^3, bound by the number of copies, not their bytes.)
+// returns.  sc_stage_wait_selftest makes the first wait run out (wait_limit
+// 0) to exercise that path.  (A first form copied each stage row with one
+// cp.async.bulk per population and row, 228 copies per stage: 20.9 GLUPS for
+// FP32 and 16-bit alike at 256^3, bound by the number of copies, not their
+// bytes.)
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -422,11 +424,17 @@ cudaError_t stage_launch(const D3Args &a, const CUtensorMap *tmap, int zc, cudaS
 }
 
 // with a tensor map: the uniform layout, TMA copies for the interior tiles;
-// without: the compact layout, every stage by cp.async
+// without: the compact layout, every stage by cp.async.  FP32 steps always
+// take the compact layout (the context builds tensor maps for 16-bit storage
+// only), so its uniform form is not instantiated.
 template <typename S, bool MOM, int PSI>
 cudaError_t stage_launch(const D3Args &a, const CUtensorMap *tmap, int zc, cudaStream_t s) {
-    return tmap ? stage_launch<S, MOM, PSI, true>(a, tmap, zc, s)
-                : stage_launch<S, MOM, PSI, false>(a, nullptr, zc, s);
+    if constexpr (sizeof(S) == 2) {
+        if (tmap) return stage_launch<S, MOM, PSI, true>(a, tmap, zc, s);
+    } else if (tmap) {
+        return cudaErrorInvalidValue;
+    }
+    return stage_launch<S, MOM, PSI, false>(a, nullptr, zc, s);
 }
 
 template <typename S>
@@ -462,12 +470,13 @@ EncodeTiled encode_tiled() {
 
 // The tensor map of the populations a step reads (a.src): dims (W, H, D, 19)
 // over population 0's array with the populations' stride as the fourth, box
-// (32 + 2E) x 10 x 1 x 1.  False when the driver cannot encode it (the step
-// then copies every stage with cp.async).
+// (32 + 2E) x 10 x 1 x 1 with E = 8 halo columns per side.  16-bit storage
+// only; false for FP32 or when the driver cannot encode it (the step then
+// copies every stage with cp.async).
 bool sc_stage_tensor_map(const D3Args &a, int storage, CUtensorMap *out) {
     const EncodeTiled enc = encode_tiled();
-    if (!enc || !sc_stage_chunk(a.W, a.H, a.D)) return false;
-    const int es = storage == 0 ? 4 : 2;
+    if (!enc || (storage != 1 && storage != 2) || !sc_stage_chunk(a.W, a.H, a.D)) return false;
+    const int es = 2;
     const long stride = (reinterpret_cast<const char *>(a.src.f[1]) -
                          reinterpret_cast<const char *>(a.src.f[0]));
     const int bw = ST_TX + 2 * (16 / es);
@@ -477,18 +486,13 @@ bool sc_stage_tensor_map(const D3Args &a, int storage, CUtensorMap *out) {
     const cuuint32_t box[4] = {(cuuint32_t)bw, ST_TY + 2, 1, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     if (stride <= 0 || stride % 16) return false;
-    const CUtensorMapDataType dt = storage == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                   : storage == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const CUtensorMapDataType dt =
+        storage == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     return enc(out, dt, 4, const_cast<float *>(a.src.f[0]), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
            CUDA_SUCCESS;
 }
-
-namespace {
-
-}  // namespace
 
 // The give-up path of the staged step on a 32 x 8 x 4 FP32 lattice: every
 // first stage wait is given no polls, so each block reports through *err,
