@@ -249,6 +249,7 @@ def run_closure(args, dist, ws, rank, local):
     closure_runs = [r for r in sw["runs"] if r["kind"] == "closure"]
     c128 = next((r for r in closure_runs if r["n"] == nf // 4), None)
     best_run = next((r for r in closure_runs if best and r["n"] == best["closure_n"]), None)
+    kfig = closure_kernel_figures(sw["runs"], best_run["n"] if best_run else nf // 4)
     line = {"metric": "closure_speedup_at_equal_ke_error",
             "value": best["speedup"] if best else None, "unit": "x", "n_gpus": ws,
             "steps": best_run["steps"] if best_run else None, "warmup": 0,
@@ -273,6 +274,7 @@ def run_closure(args, dist, ws, rank, local):
                        "ke_error": "RMS over the samples of E/E0 against the filtered fine run",
                        "headline": "best speed-up among closure runs with KE error <= %g"
                                    % cfg["max_ke_error"]},
+            "roofline": kfig[0], "mlp_time": kfig[1],
             "closure": {"equal_error_pairs": pairs, "best": best, "runs": sw["runs"],
                         "fine_seconds": sw["fine_seconds"], "fine_steps": sw["fine_steps"],
                         "closure_128_vs_fine_run": (sw["fine_seconds"] / c128["seconds"])
@@ -289,6 +291,53 @@ def measured_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+FALLBACK_BF16_TFLOPS_SUSTAINED = 1700.0
+
+
+def measured_tensor_peak():
+    """Dense BF16 tensor throughput for a kernel timed inside a long run (the
+    sustained figure)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops_sustained"]), "measured"
+    except Exception:
+        return FALLBACK_BF16_TFLOPS_SUSTAINED, "fallback"
+
+
+# learned closure: 2 (19*64 + 64*64 + 64) FLOP of the network per cell
+CLOSURE_FLOP_PER_CELL = 2 * (19 * 64 + 64 * 64 + 64)
+
+
+def closure_kernel_figures(runs, n):
+    """The closure step kernel on the n^3 grid: its time per step beside the
+    plain step's on the same grid (the difference is the network's share),
+    and its roofline: 153 algorithmic bytes per cell against HBM and the
+    network's FLOP against the sustained BF16 tensor peak."""
+    cl = next((r for r in runs if r["kind"] == "closure" and r["n"] == n), None)
+    pl = next((r for r in runs if r["kind"] == "plain" and r["n"] == n), None)
+    if cl is None:
+        return None, None
+    cells = n ** 3
+    t_cl = cl["seconds"] / cl["steps"]
+    hbm, hbm_kind = measured_peak()
+    tc, tc_kind = measured_tensor_peak()
+    gbs = 153.0 * cells / t_cl / 1e9
+    tflops = CLOSURE_FLOP_PER_CELL * cells / t_cl / 1e12
+    roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+            "peak_source": hbm_kind, "bytes_per_lu": 153, "traffic": None,
+            "kernel": "d3q19_closure_tc_kernel", "grid": n,
+            "tensor": {"achieved": tflops, "peak": tc, "unit": "TFLOP/s", "frac": tflops / tc,
+                       "peak_source": tc_kind + " (sustained)",
+                       "flop_per_cell": CLOSURE_FLOP_PER_CELL}}
+    mlp = {"grid": n, "closure_ms_per_step": 1e3 * t_cl,
+           "plain_ms_per_step": 1e3 * pl["seconds"] / pl["steps"] if pl else None}
+    if pl:
+        mlp["network_ms_per_step"] = mlp["closure_ms_per_step"] - mlp["plain_ms_per_step"]
+        mlp["network_share_of_step"] = mlp["network_ms_per_step"] / mlp["closure_ms_per_step"]
+    return roof, mlp
 
 
 class ClockSampler:
