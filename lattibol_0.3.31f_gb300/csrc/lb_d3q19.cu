@@ -30,8 +30,13 @@ namespace lb {
 // the density pass of this step, applied as a velocity shift F/(tau_inv rho)
 // like the reference's force (src/collision.cu:92-96).
 // ---------------------------------------------------------------------------
+// 16-bit storage without Shan-Chen waits on its loads, not on issue: it runs
+// at least 12 blocks per SM (40 registers, a 24-byte spill; 64.0 vs 62.4
+// GLUPS on the 256x128x128 channel, FP16), FP32 at its own register count
+// (46.0 vs 44.2 GLUPS when held to 12 blocks)
 template <int MODE, bool MOM, bool PLOT, typename S, bool SC>
-__global__ void __launch_bounds__(D3_BLOCK) d3q19_fused_kernel(const D3Args a) {
+__global__ void __launch_bounds__(D3_BLOCK, (sizeof(S) == 2 && !SC) ? 12 : 0)
+    d3q19_fused_kernel(const D3Args a) {
     const Coord3 c(a);
     const int x = c.x, y = c.y, z = c.z;
     if (x >= a.W) return;
