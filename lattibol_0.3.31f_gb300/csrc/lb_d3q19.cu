@@ -30,10 +30,19 @@ namespace lb {
 // the density pass of this step, applied as a velocity shift F/(tau_inv rho)
 // like the reference's force (src/collision.cu:92-96).
 // ---------------------------------------------------------------------------
-// 16-bit storage without Shan-Chen waits on its loads, not on issue: it runs
-// at least 12 blocks per SM (40 registers, a 24-byte spill; 64.0 vs 62.4
-// GLUPS on the 256x128x128 channel, FP16), FP32 at its own register count
-// (46.0 vs 44.2 GLUPS when held to 12 blocks)
+// 16-bit storage without Shan-Chen waits on its loads, not on issue.  Two
+// things put more of them in flight:
+//  * at least 12 blocks per SM (40 registers, a 24-byte spill; 64.0 vs 62.4
+//    GLUPS on the 256x128x128 channel, FP16); FP32 keeps its own register
+//    count (46.0 vs 44.2 GLUPS when held to 12 blocks);
+//  * an L2 prefetch of the populations the block FUSED_PF_BLOCKS later in the
+//    sweep pulls: its two 128-byte lines of each of the 19 arrays (66.8 vs
+//    63.4 GLUPS; 608 to 1520 blocks ahead measured alike, 3648 lost the gain;
+//    prefetching that block's flags as well, or pulling before testing the
+//    node's flags, measured no faster).
+constexpr long FUSED_PF_BLOCKS = 912;
+static_assert(D3_BLOCK * 2 == 256, "two 128-byte lines per 16-bit population run");
+
 template <int MODE, bool MOM, bool PLOT, typename S, bool SC>
 __global__ void __launch_bounds__(D3_BLOCK, (sizeof(S) == 2 && !SC) ? 12 : 0)
     d3q19_fused_kernel(const D3Args a) {
@@ -41,6 +50,16 @@ __global__ void __launch_bounds__(D3_BLOCK, (sizeof(S) == 2 && !SC) ? 12 : 0)
     const int x = c.x, y = c.y, z = c.z;
     if (x >= a.W) return;
     const int o = x + a.W * (y + a.H * z);
+    if (sizeof(S) == 2 && MODE == MODE_NATIVE && !SC && threadIdx.x < 19 * 2) {
+        // L2 prefetch: line (threadIdx.x & 1) of population threadIdx.x / 2's
+        // run of the block FUSED_PF_BLOCKS later in the sweep
+        const int k = threadIdx.x >> 1, l = threadIdx.x & 1;
+        const long po = ((long)o - threadIdx.x) +
+                        (a.reverse ? -1L : 1L) * FUSED_PF_BLOCKS * blockDim.x + l * 64;
+        if (po >= 0 && po < (long)a.W * a.H * a.D)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const S *>(a.src.f[k]) +
+                                                           po));
+    }
     const uint8_t fl = a.flags[o];
     const Nbr3 n(x, y, z, a.W, a.H, a.D);
 
