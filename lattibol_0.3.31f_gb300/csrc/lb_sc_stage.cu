@@ -42,8 +42,8 @@
 // in 16-bit storage, their deviation forms; d3q19_sc_sum_native), so the
 // result is bit-identical to the density pass + fused step.
 //
-// Every mbarrier wait is bounded (wait_limit polls of about a microsecond for
-// a stage; ST_WAIT in the library's launches); a block that gives up raises
+// Every mbarrier wait is bounded (wait_limit polls for a stage; ST_WAIT in the
+// library's launches); a block that gives up raises
 // the device error word, waits (bounded by ST_WAIT) for the stages it still
 // has in flight, drains its threads' own copies (cp.async.wait_all) and
 // returns.  sc_stage_wait_selftest makes the first wait run out (wait_limit

@@ -89,18 +89,20 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
 __device__ __forceinline__ void mbar_inval(uint64_t *mbar) {
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_u32(mbar)) : "memory");
 }
-// waits for the phase with the given parity; false after `limit` attempts of
-// at most about 1 us each (the suspend-time hint), so the bound is in time
+// waits for the phase with the given parity; false after `limit` attempts.
+// Each attempt may suspend the thread for a time the hardware chooses (no
+// suspend-time hint: with a 1 us hint a stream of bulk copies ran 12 % slower,
+// the staged Shan-Chen step 1 %), so the bound is a count of attempts.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int limit) {
     const uint32_t a = smem_u32(mbar);
     for (int i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity), "r"(1000u)
+            : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
     }
