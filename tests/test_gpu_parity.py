@@ -396,3 +396,36 @@ def test_full_size_channel_steps_vs_oracle(pkg, oracle):
     rho_g, ux_g, uy_g, uz_g = lat.moments()
     assert beq(rho_g, mom[3]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1]) and beq(uz_g, mom[2])
     lat.close()
+
+
+@pytest.mark.parametrize("storage", [1, 2], ids=["f16", "bf16"])
+def test_full_size_channel_16bit_vs_oracle(pkg, oracle, storage):
+    """The same 65 steps of the bench lattice in 16-bit deviation storage
+    (rho_ref 1): the library's default 16-bit step at this size -- its L2
+    prefetch of the rows 912 blocks ahead reaches real rows only on a lattice
+    this large -- against the oracle with the storage emulated, every bit of
+    every fluid node and the last step's moments."""
+    from storage_emul import Emulated
+    W, H, D = 256, 128, 128
+    N = W * H * D
+    steps = 65
+    flags = _channel_flags(W, H, D, sphere=(64, 64, 64, 16))
+    tau_inv = np.float32(1 / 0.55)
+    F = (np.float32(1e-6), np.float32(0), np.float32(0))
+    rng = np.random.default_rng(2027 + storage)
+    rho = (1 + 0.01 * rng.standard_normal(N)).astype(np.float32)
+    u = [(0.02 * rng.standard_normal(N)).astype(np.float32) for _ in range(3)]
+    f0 = oracle.d3q19_equilibrium(rho, *u, *pkg.W3)
+    lat = pkg.Lattice(19, W, H, D, tau_inv=tau_inv, force=F, storage=storage, rho_ref=1.0)
+    lat.set_flags(flags)
+    lat.set_populations(f0)
+    lat.step(steps)
+    em = Emulated(oracle, f0, storage, 1.0)
+    mom = [np.zeros(N, np.float32) for _ in range(4)]
+    for _ in range(steps):
+        em.step(flags, np.zeros(19, np.float32), W, H, D, mom, pkg.W3, tau_inv, F)
+    fluid = (flags & 1) == 0
+    assert beq(lat.populations()[:, fluid], em.populations()[:, fluid])
+    rho_g, ux_g, uy_g, uz_g = lat.moments()
+    assert beq(rho_g, mom[3]) and beq(ux_g, mom[0]) and beq(uy_g, mom[1]) and beq(uz_g, mom[2])
+    lat.close()
