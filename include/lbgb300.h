@@ -169,14 +169,6 @@ typedef enum {
 /* launch tuning (lb_config.tuning); results do not depend on it */
 #define LB_TUNE_DEFAULT 0      /* the library's measured choice */
 #define LB_TUNE_EXPLICIT 0x100 /* use exactly the bits below */
-#define LB_TUNE_PERSISTENT 0x004 /* D2Q9 without Shan-Chen: lb_step runs all its steps
-                                    in one cooperative launch whose blocks own row
-                                    bands and wait (bounded) only for their two
-                                    neighbour bands; for lattices whose step is
-                                    shorter than a launch */
-#define LB_TUNE_CLOSURE_MMA_SYNC 0x010 /* learned closure: evaluate the network with the
-                                          warp-level mma.sync kernel instead of the
-                                          tcgen05 (tensor memory) kernel */
 #define LB_TUNE_PDL 0x008      /* D2Q9 without Shan-Chen: each step is a programmatic
                                   dependent launch of the previous one, so its launch
                                   overlaps the previous step's tail */
@@ -357,9 +349,8 @@ int lb_device_fields(lb_ctx *ctx, float **rho, float **ux, float **uy, float **u
  * W2[n][k] = (n + 2k) mod 5 - 2, k < 64 (exact small integers).  *status
  * gets bit 2i (bit 2i+1) when round i's first (second) MMA never completed. */
 int lb_tcgen05_selftest(float *out, int *status);
-/* self-check of the bounded waits on the GPU: which = 0 makes the persistent
- * D2Q9 loop's band wait run out (a counter that nothing raises), which = 1 the
- * tcgen05 kernels' mbarrier wait (nothing committed), which = 2 the staged
+/* self-check of the bounded waits on the GPU: which = 1 makes the tcgen05
+ * kernels' mbarrier wait run out (nothing committed), which = 2 the staged
  * Shan-Chen step's stage wait (given no polls; the block then waits for the
  * copies it issued before it returns).  *status = 1 when the wait gave up as
  * designed, reported the failure and returned. */

@@ -94,7 +94,7 @@ LB_PSI_REF, LB_PSI_EXP1 = 0, 1
 LB_CELL_FLUID, LB_CELL_WALL, LB_CELL_MOVING = 0, 1, 2
 LB_ABI_STANDALONE, LB_ABI_FUSED = 0, 1
 LB_TUNE_DEFAULT, LB_TUNE_EXPLICIT, LB_TUNE_REVERSE = 0, 0x100, 0x001
-LB_TUNE_PERSISTENT, LB_TUNE_PDL, LB_TUNE_CLOSURE_MMA_SYNC = 0x004, 0x008, 0x010
+LB_TUNE_PDL = 0x008
 LB_TUNE_TBLOCK = 0x020
 LB_TUNE_SC_STAGED = 0x040
 LB_TUNE_SC_NO_TMA = 0x080

@@ -1,12 +1,12 @@
 // lb_closure.cu -- learned sub-grid closure for under-resolved D3Q19 flow.
 //
-// * d3q19_closure_kernel: the fused native D3Q19 step in which every cell's
+// * d3q19_closure_tc_kernel: the fused native D3Q19 step in which every cell's
 //   relaxation time comes from the closure network.  Per cell it forms 19
 //   features from the pre-collision populations -- the 18 non-conserved
 //   non-equilibrium moments (momentum 3, stress 6, third/fourth order 9 in
 //   the raw basis c_x c_y^2, ..., c_y^2 c_z^2) scaled by 1/(rho c_s^2 tau0
 //   s_ref), and |S| / s_ref with S = -Pi_neq / (2 rho c_s^2 tau0) -- and the
-//   warp evaluates the network for its 32 cells on the tensor cores.  The
+//   block evaluates the network for its 128 cells on the tensor cores.  The
 //   output y gives nu_t = nu0 * clamp(y, 0, z_max) and tau = 0.5 + 3 (nu0 +
 //   nu_t).
 // * filter / feature kernels: box-filter a fine lattice's moments onto a
@@ -15,9 +15,10 @@
 //   the filtered velocity; the other moments are zero at first order) and
 //   the target z = nu_t/nu0 of the local least-squares eddy viscosity of the
 //   filtered sub-grid stress, nu_t = max(0, -(T_dev : S) / (2 S : S)).
-// * training: the forward pass of the closure kernel (tensor cores), an FP32
-//   backward pass per sample, per-block weight-gradient sums in shared
-//   memory, a fixed-order reduction of the block partials, and Adam.
+// * training: forward and backward passes over 128-sample tiles with every
+//   contraction on the tensor cores (mlp_tc_kernel), per-block gradient sums
+//   accumulated in tensor memory, a fixed-order reduction of the block
+//   partials, and Adam.
 #include <algorithm>
 #include <cstddef>
 #include <cmath>
@@ -95,74 +96,10 @@ __device__ __forceinline__ void closure_features(const float (&g)[19], float rho
                             2.f * (sxy * sxy + sxz * sxz + syz * syz)));
 }
 
-// fused native D3Q19 step with the closure (F32 storage)
-// Persistent: each block stages the network once and then walks row-blocks
-// of D3_BLOCK cells (x-run at fixed y, z) with a stride of the grid size.
-template <bool MOM>
-__global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
-                                                                 const ClosureArgs ca) {
-    __shared__ MlpSmemWeights sW;
-    __shared__ MlpSmemWarp sWarp[D3_BLOCK / 32];
-    mlp_load_weights(sW, ca.mlp);
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    MlpSmemWarp &sw = sWarp[threadIdx.x >> 5];
-    const int nbx = (a.W + D3_BLOCK - 1) / D3_BLOCK;
-    const long nrows = (long)nbx * a.H * a.D;
-    for (long r = blockIdx.x; r < nrows; r += gridDim.x) {
-        const long rr = a.reverse ? nrows - 1 - r : r;
-        const int bx = (int)(rr % nbx);
-        const long yz = rr / nbx;
-        const int y = (int)(yz % a.H), z = (int)(yz / a.H);
-        const int x = bx * D3_BLOCK + threadIdx.x;
-        const bool inside = x < a.W;
-        const int o = inside ? x + a.W * (y + a.H * z) : 0;
-        const uint8_t fl = inside ? a.flags[o] : CELL_WALL;
-        const bool fluid = !(fl & CELL_WALL);
-        float g[19], rho = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
-        float feat[MLP_IN];
-#pragma unroll
-        for (int i = 0; i < MLP_IN; i++) feat[i] = 0.f;
-        if (fluid) {
-            const Nbr3 n(x, y, z, a.W, a.H, a.D);
-            pull_native<float>(a, o, n, fl, g);
-            d3q19_moments_native(g, rho, ux, uy, uz);
-            closure_features(g, rho, ux, uy, uz, ca.tau0, ca.s_ref, feat);
-        }
-        __nv_bfloat162 *row = reinterpret_cast<__nv_bfloat162 *>(sw.x + lane * SX_STRIDE);
-#pragma unroll
-        for (int i = 0; i < MLP_IN_PAD / 2; i++)
-            row[i] = __floats2bfloat162_rn(2 * i < MLP_IN ? feat[2 * i] : 0.f,
-                                           2 * i + 1 < MLP_IN ? feat[2 * i + 1] : 0.f);
-        mlp_output_warp(sW, sw);
-        const float yv = sw.y[lane];
-        if (!inside) continue;
-        if (!fluid) {
-            if (MOM) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.uz[o] = 0.f; a.rho[o] = 0.f; }
-            if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
-            continue;
-        }
-        if (ca.y_out) ca.y_out[o] = yv;
-        const float zt = fminf(fmaxf(yv, 0.f), ca.z_max);
-        const float tau_inv = 1.f / (0.5f + 3.f * (ca.nu0 + ca.nu0 * zt));
-        if (MOM) { a.ux[o] = ux; a.uy[o] = uy; a.uz[o] = uz; a.rho[o] = rho; }
-        if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, uz, rho);
-        float ex = ux, ey = uy, ez = uz;
-        if (a.Fx != 0.f || a.Fy != 0.f || a.Fz != 0.f) {
-            const float inv_rt = 1.f / (rho * tau_inv);
-            if (a.Fx != 0.f) ex = __fmaf_rn(a.Fx, inv_rt, ux);
-            if (a.Fy != 0.f) ey = __fmaf_rn(a.Fy, inv_rt, uy);
-            if (a.Fz != 0.f) ez = __fmaf_rn(a.Fz, inv_rt, uz);
-        }
-        d3q19_bgk_native(g, ex, ey, ez, rho, a.w0, a.w1, a.w7, tau_inv);
-#pragma unroll
-        for (int k = 0; k < 19; k++) a.dst.f[k][o] = g[k];
-    }
-}
-
 // ---------------------------------------------------------------------------
-// The same step with the network on the 5th-generation tensor cores.  A block
-// of 128 threads takes a run of 128 cells; thread t owns cell t, row t of the
+// The fused native D3Q19 step (F32 storage) with the network on the
+// 5th-generation tensor cores.  A block of 128 threads takes a run of 128
+// cells; thread t owns cell t, row t of the
 // MMA tiles and lane t of tensor memory.  Per run:
 //   1. every thread writes its 19 BF16 features (padded to 32) as row t of A
 //      (K-major 8x8 core matrices, lb_tc05.cuh);
@@ -173,10 +110,9 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_kernel(const D3Args a,
 //   4. thread 0 issues D = H W2^T (four k16 MMAs) into the same columns;
 //   5. each thread loads its row, adds b2, applies ReLU and sums w3 h + b3
 //      (fused multiply-adds).
-// Rounding points are the warp-level kernel's (BF16 inputs, weights and
-// first hidden layer; FP32 accumulation, biases and last layer) except that
-// the last layer's products are fused into the sum (one rounding each, not
-// two).
+// Rounding points (restated by the numpy oracle): BF16 inputs, weights and
+// first hidden layer; FP32 accumulation, biases and last layer, whose
+// products are fused into the sum.
 // ---------------------------------------------------------------------------
 // ReLU and round-to-nearest BF16 of two floats in one conversion, lo in the
 // low half (the PTX packs its first source into the high half)
@@ -384,44 +320,28 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
 
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s) {
-    if (!ca.legacy_mma) {
-        // SMs x resident blocks.  The occupancy query reports one block per SM
-        // for a kernel that allocates tensor memory, so the residency is
-        // computed from the kernel's registers and shared memory, and capped
-        // at 8 blocks (8 x 64 of the SM's 512 tensor-memory columns).
-        static int tc_cap = 0;
-        if (!tc_cap) {
-            int dev = 0, sms = 1, smem_sm = 0, thr_sm = 2048;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-            cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
-            cudaFuncAttributes fa{};
-            cudaFuncGetAttributes(&fa, d3q19_closure_tc_kernel<false>);
-            const int regs = std::max(1, (fa.numRegs + 7) / 8 * 8 * D3_BLOCK);
-            int occ = std::min({65536 / regs, thr_sm / D3_BLOCK,
-                                smem_sm / (int)(fa.sharedSizeBytes + 1024), 512 / TC_COLS});
-            tc_cap = sms * std::max(occ, 1);
-        }
-        const long nrows = ((long)a.W * a.H * a.D + D3_BLOCK - 1) / D3_BLOCK;
-        const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
-        if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
-        else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
-        return cudaGetLastError();
-    }
-    static int grid_cap = 0;  // SMs x resident blocks of the kernel, computed once
-    if (!grid_cap) {
-        int dev = 0, sms = 1, occ = 1;
+    // SMs x resident blocks.  The occupancy query reports one block per SM
+    // for a kernel that allocates tensor memory, so the residency is
+    // computed from the kernel's registers and shared memory, and capped
+    // at 8 blocks (8 x 64 of the SM's 512 tensor-memory columns).
+    static int tc_cap = 0;
+    if (!tc_cap) {
+        int dev = 0, sms = 1, smem_sm = 0, thr_sm = 2048;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, d3q19_closure_kernel<false>,
-                                                      D3_BLOCK, 0);
-        grid_cap = sms * (occ > 0 ? occ : 1);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, d3q19_closure_tc_kernel<false>);
+        const int regs = std::max(1, (fa.numRegs + 7) / 8 * 8 * D3_BLOCK);
+        int occ = std::min({65536 / regs, thr_sm / D3_BLOCK,
+                            smem_sm / (int)(fa.sharedSizeBytes + 1024), 512 / TC_COLS});
+        tc_cap = sms * std::max(occ, 1);
     }
-    const long nrows = (long)((a.W + D3_BLOCK - 1) / D3_BLOCK) * a.H * a.D;
-    const unsigned g = (unsigned)(nrows < grid_cap ? nrows : grid_cap);
-    if (mom) d3q19_closure_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
-    else d3q19_closure_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
+    const long nrows = ((long)a.W * a.H * a.D + D3_BLOCK - 1) / D3_BLOCK;
+    const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
+    if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
+    else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
     return cudaGetLastError();
 }
 
@@ -541,250 +461,446 @@ __global__ void features_kernel(const float *fl, int Wc, int Hc, int Dc, float n
     fo[18] = sqrtf(2.f * fc.SS) / s_ref;
 }
 
-// ------------------------------------------------------------------ training
-constexpr int HROW = MLP_H + 1;
-struct TrainSmemWarp {
-    MlpSmemWarp m;                         // x and the first hidden layer (BF16), y
-    float h2[32 * HROW];                   // row stride 65: a warp walking its rows hits 32 banks
-    float dh2[32 * HROW];
-    float dh1[32 * HROW];
-    __nv_bfloat16 dh2b[32 * SH_STRIDE];    // BF16 copies: operands of the gradient MMAs
-    __nv_bfloat16 dh1b[32 * SH_STRIDE];
-    float dy[32];
-};
-constexpr int TRAIN_WARPS = 4;
+// ------------------------------------------------------------------ network
+// The network's forward pass and, for training, its backward pass over tiles
+// of 128 samples on the 5th-generation tensor cores.  Thread t owns sample t
+// of a tile, row t of the sample-major MMA tiles, column t of the transposed
+// (sample-contracted) tiles and lane t of tensor memory.  Thread 0 issues
+// every MMA (BF16 operands in shared memory, K-major core matrices,
+// lb_tc05.cuh; FP32 accumulators in tensor memory) and commits it to one
+// mbarrier.  Per tile:
+//   1. x (19 features, padded to 32) -> row t of A; D_h1 = A W1^T;
+//   2. h1 = ReLU(D_h1 + b1) as BF16 -> row t of A (K 64) and column t of
+//      H1^T; D_h2 = A W2^T;
+//   3. h2 = ReLU(D_h2 + b2), y = b3 + sum_j w3_j h2_j (paired FP32, as the
+//      closure kernel).  Forward only: y is the output.  Training:
+//      dy = 2 (y - z) / n, dH2 = dy w3 (h2 > 0) as BF16 -> row t of A and
+//      column t of dH2^T; h2 and dy as BF16 -> column t of H2^T and of dY;
+//      D_dh1 = dH2 W2 (B = W2^T);
+//   4. dH1 = D_dh1 (h1 > 0) as BF16 -> column t of dH1^T; then two MMAs
+//      contract over the tile's samples into accumulators that persist
+//      across the block's tiles:
+//        G  = [dH2^T; dH1^T] [H1^T; X^T; 1]^T  (M 128, N 96): dW2 = G[0:64,
+//             0:64], dW1 = G[64:128, 64:83], db2 = G[0:64, 83], db1 =
+//             G[64:128, 83] (the other blocks of G are not read);
+//        G3 = [H2^T; 1] dY^T  (M 128, N 16): dw3 = G3[0:64, 0], db3 = G3[64, 0].
+// After its last tile each block writes its sums, already divided by n, and
+// its loss sum to partial[block][NGRAD].
+// Rounding points (restated by the numpy oracle): x, W1, W2, h1 enter the
+// forward MMAs as BF16; dH2, dH1, h1, x, h2 and dy enter the gradient MMAs
+// as BF16; every accumulation is FP32.
+namespace net {
+constexpr int OFF_W1 = 0;                               // W1 [64][32]: B of layer 1
+constexpr int OFF_W2 = OFF_W1 + MLP_H * MLP_IN_PAD * 2; // W2 [j][i]: B of layer 2
+constexpr int OFF_A = OFF_W2 + MLP_H * MLP_H * 2;       // x (K 32), h1, then dH2 (K 64)
+constexpr int OFF_F = OFF_A + 128 * MLP_H * 2;          // b1, b2, w3, b3, loss, mbarrier, slot
+constexpr int FWD_SMEM = OFF_F + 1024;
+constexpr int OFF_W2T = FWD_SMEM;                       // W2^T [i][j]: B of dH1 = dH2 W2
+constexpr int OFF_GA = OFF_W2T + MLP_H * MLP_H * 2;     // [dH2^T; dH1^T] [128][128 samples]
+constexpr int OFF_GB = OFF_GA + 128 * 128 * 2;          // [H1^T; X^T; 1; 0] [96][128]
+constexpr int OFF_HA = OFF_GB + 96 * 128 * 2;           // [H2^T; 1; 0] [128][128]
+constexpr int OFF_DY = OFF_HA + 128 * 128 * 2;          // [dY; 0] [16][128]
+constexpr int TRAIN_SMEM = OFF_DY + 16 * 128 * 2;
+// tensor-memory columns
+constexpr uint32_t COL_H1 = 0, COL_H2 = 64, COL_G = 128, COL_G3 = 224;
+constexpr int ROW_ONES = 64 + MLP_IN;  // the row of ones in [H1^T; X^T; 1; 0]
+static_assert(OFF_F % 16 == 0 && OFF_GA % 16 == 0 && OFF_GB % 16 == 0 && OFF_HA % 16 == 0 &&
+                  OFF_DY % 16 == 0 && TRAIN_SMEM <= 227 * 1024,
+              "descriptor start addresses on 16 bytes; one block fits the SM");
+static_assert(COL_G3 + 16 <= 256 && ROW_ONES < 96, "tensor-memory and tile extents");
+}  // namespace net
 constexpr int NGRAD = MLP_NPARAM + 1;  // + loss
-// the per-warp tiles start on a 128-byte boundary after the weights
-constexpr size_t TRAIN_WARP_OFF = (sizeof(MlpSmemWeights) + 127) / 128 * 128;
-constexpr size_t TRAIN_SMEM =
-    TRAIN_WARP_OFF + TRAIN_WARPS * sizeof(TrainSmemWarp) + NGRAD * sizeof(float);
-static_assert(offsetof(MlpSmemWeights, w2) % 16 == 0 && sizeof(MlpSmemWarp) % 16 == 0 &&
-                  (32 * HROW * sizeof(float)) % 16 == 0 && sizeof(TrainSmemWarp) % 16 == 0,
-              "ldmatrix rows stay 16-byte aligned");
+constexpr int NET_FWD_SMEM = 50 * 1024;  // at most 4 blocks (4 x 128 columns) per SM
 
-// Forward (mma.sync, as mlp_forward_warp) and backward over the samples
-// [0, n) of a batch, every contraction on the tensor cores (mma.sync
-// m16n8k16, BF16 operands, FP32 accumulate).  A block takes 128 samples at a
-// time, 32 per warp:
-//  * per warp: dy = 2 (y - z) / n per sample, dH2 = dy w3 (h2 > 0) from the
-//    second layer's accumulator fragments, dH1 = (dH2 W2) (h1 > 0) -- dH2 and
-//    W2 as BF16 operands (W2 read transposed by ldmatrix .trans);
-//  * per block (after a barrier): warp w owns rows 16w .. 16w+15 of dW2 =
-//    dH2^T H1 and of dW1 = dH1^T X, contracting over all 128 samples in a
-//    fixed order (both operands read transposed by ldmatrix .trans), and adds
-//    them into the block's gradient sums, every element owned by one thread;
-//  * the bias and output-layer gradients (db1, db2, dw3, db3) are FP32 sums
-//    over the samples, each parameter owned by one thread.
-// Rounding points (restated by the numpy oracle): dH2 and dH1 enter the MMAs
-// as BF16; everything is accumulated in FP32.  Each block leaves its gradient
-// sums (already divided by n) and its loss sum in partial[block][NGRAD].
-__global__ void __launch_bounds__(32 * TRAIN_WARPS) mlp_train_kernel(
-    MlpDev mlp, const float *X, const float *Z, long n, float *partial) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    MlpSmemWeights &sW = *reinterpret_cast<MlpSmemWeights *>(smem);
-    TrainSmemWarp *sWarp = reinterpret_cast<TrainSmemWarp *>(smem + TRAIN_WARP_OFF);
-    float *sG = reinterpret_cast<float *>(smem + TRAIN_WARP_OFF +
-                                          TRAIN_WARPS * sizeof(TrainSmemWarp));
-    mlp_load_weights(sW, mlp);
-    for (int i = threadIdx.x; i < NGRAD; i += blockDim.x) sG[i] = 0.f;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    TrainSmemWarp &tw = sWarp[wid];
-    const int g = lane >> 2, t = lane & 3;
-    const float inv_n = 1.f / (float)n;
-    // ldmatrix row addresses: (row, column) of this lane in the four 8x8 matrices
-    // of a 16x16 tile read as [k-rows 0-7 | 8-15] x [n-columns 0-7 | 8-15]
-    const int lr_b = (lane & 7) + 8 * ((lane >> 3) & 1), lc_b = 8 * (lane >> 4);
-    //   ... and as [m-columns 0-7 | 8-15] x [k-rows 0-7 | 8-15] (A from a stored
-    //   [k][m] matrix)
-    const int lr_a = (lane & 7) + 8 * (lane >> 4), lc_a = 8 * ((lane >> 3) & 1);
-    __syncthreads();
-    for (long base = (long)blockIdx.x * 32 * TRAIN_WARPS; base < n;
-         base += (long)gridDim.x * 32 * TRAIN_WARPS) {
-        const long s = base + wid * 32 + lane;
-        const bool valid = s < n;
-        for (int i = 0; i < MLP_IN_PAD; i++)
-            tw.m.x[lane * SX_STRIDE + i] =
-                __float2bfloat16_rn((valid && i < MLP_IN) ? X[s * MLP_IN + i] : 0.f);
-        float h2[2][8][4];
-        mlp_forward_warp(sW, tw.m, h2, true);
-        const float err = valid ? tw.m.y[lane] - Z[s] : 0.f;
-        tw.dy[lane] = 2.f * err * inv_n;
-        __syncwarp();
-        // dH2 = dy w3 (h2 > 0), from the accumulator fragments
+__device__ __forceinline__ void st_b16(uint8_t *base, uint32_t off, uint32_t bits) {
+    *reinterpret_cast<uint16_t *>(base + off) = (uint16_t)bits;
+}
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+    const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&p);
+}
+// Rows r0 .. r0+3 (r0 a multiple of 4) of column t of a sample-contracted
+// tile (K = 128 samples), from w01 (rows r0, r0+1 in its low, high half) and
+// w23.  The four 8-lane groups of a warp start at different rows, so the four
+// 16-byte pieces of each store instruction fall in different banks.
+__device__ __forceinline__ void st_col4(uint8_t *tile, int r0, int t, uint32_t w01,
+                                        uint32_t w23) {
+    const int g = (t >> 3) & 3;
+    const uint32_t off = kmajor_offset(r0, t, 128);
 #pragma unroll
-        for (int mt = 0; mt < 2; mt++) {
-            const int r0 = mt * 16 + g, r1 = r0 + 8;
-            const float dy0 = tw.dy[r0], dy1 = tw.dy[r1];
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const int c0 = nt * 8 + 2 * t;
-                const float *q = h2[mt][nt];
-                const float d00 = q[0] > 0.f ? dy0 * sW.w3[c0] : 0.f;
-                const float d01 = q[1] > 0.f ? dy0 * sW.w3[c0 + 1] : 0.f;
-                const float d10 = q[2] > 0.f ? dy1 * sW.w3[c0] : 0.f;
-                const float d11 = q[3] > 0.f ? dy1 * sW.w3[c0 + 1] : 0.f;
-                tw.h2[r0 * HROW + c0] = q[0];
-                tw.h2[r0 * HROW + c0 + 1] = q[1];
-                tw.h2[r1 * HROW + c0] = q[2];
-                tw.h2[r1 * HROW + c0 + 1] = q[3];
-                tw.dh2[r0 * HROW + c0] = d00;
-                tw.dh2[r0 * HROW + c0 + 1] = d01;
-                tw.dh2[r1 * HROW + c0] = d10;
-                tw.dh2[r1 * HROW + c0 + 1] = d11;
-                *reinterpret_cast<__nv_bfloat162 *>(tw.dh2b + r0 * SH_STRIDE + c0) =
-                    __floats2bfloat162_rn(d00, d01);
-                *reinterpret_cast<__nv_bfloat162 *>(tw.dh2b + r1 * SH_STRIDE + c0) =
-                    __floats2bfloat162_rn(d10, d11);
-            }
-        }
-        __syncwarp();
-        // dH1 = (dH2 W2) (h1 > 0): A = dH2 [samples x 64], B[k = j][n = i] = W2[j][i]
-#pragma unroll 1
-        for (int mt = 0; mt < 2; mt++) {
-            float acc[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-#pragma unroll
-            for (int kt = 0; kt < 4; kt++) {
-                const __nv_bfloat16 *da = tw.dh2b + (mt * 16 + g) * SH_STRIDE + kt * 16 + 2 * t;
-                const uint32_t a[4] = {ld_b32(da), ld_b32(da + 8 * SH_STRIDE), ld_b32(da + 8),
-                                       ld_b32(da + 8 * SH_STRIDE + 8)};
-#pragma unroll
-                for (int np = 0; np < 4; np++) {
-                    uint32_t b[4];
-                    ldsm_x4_trans(b, sW.w2 + (kt * 16 + lr_b) * SW2_STRIDE + np * 16 + lc_b);
-                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
-                    mma_bf16_16816(acc[2 * np], a, b0);
-                    mma_bf16_16816(acc[2 * np + 1], a, b1);
-                }
-            }
-            const int r0 = mt * 16 + g, r1 = r0 + 8;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const int c0 = nt * 8 + 2 * t;
-                const __nv_bfloat16 *h1r0 = tw.m.h1 + r0 * SH_STRIDE + c0;
-                const __nv_bfloat16 *h1r1 = tw.m.h1 + r1 * SH_STRIDE + c0;
-                const float d00 = __bfloat162float(h1r0[0]) > 0.f ? acc[nt][0] : 0.f;
-                const float d01 = __bfloat162float(h1r0[1]) > 0.f ? acc[nt][1] : 0.f;
-                const float d10 = __bfloat162float(h1r1[0]) > 0.f ? acc[nt][2] : 0.f;
-                const float d11 = __bfloat162float(h1r1[1]) > 0.f ? acc[nt][3] : 0.f;
-                tw.dh1[r0 * HROW + c0] = d00;
-                tw.dh1[r0 * HROW + c0 + 1] = d01;
-                tw.dh1[r1 * HROW + c0] = d10;
-                tw.dh1[r1 * HROW + c0 + 1] = d11;
-                *reinterpret_cast<__nv_bfloat162 *>(tw.dh1b + r0 * SH_STRIDE + c0) =
-                    __floats2bfloat162_rn(d00, d01);
-                *reinterpret_cast<__nv_bfloat162 *>(tw.dh1b + r1 * SH_STRIDE + c0) =
-                    __floats2bfloat162_rn(d10, d11);
-            }
-        }
-        // block loss: sum over the warp, one atomic per warp into shared memory
-        float e2 = err * err;
-        for (int d = 16; d > 0; d >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, d);
-        if (lane == 0) atomicAdd(&sG[MLP_NPARAM], e2 * inv_n);
-        __syncthreads();
-        // dW2 rows j = 16 wid .. 16 wid + 15 (all 64 columns) and dW1 rows
-        // i = 16 wid .. (inputs 0..31) over the block's 128 samples: k-step kk
-        // is samples 16 kk .. 16 kk + 15, rows 16 (kk & 1) .. of warp kk / 2's tiles
-        {
-            float a2[8][4], a1[4][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) a2[nt][0] = a2[nt][1] = a2[nt][2] = a2[nt][3] = 0.f;
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) a1[nt][0] = a1[nt][1] = a1[nt][2] = a1[nt][3] = 0.f;
-#pragma unroll 1
-            for (int kk = 0; kk < 2 * TRAIN_WARPS; kk++) {
-                const TrainSmemWarp &u = sWarp[kk >> 1];
-                const int sr = (kk & 1) * 16;
-                uint32_t a[4];
-                // A[m = j][k = sample] = dH2[sample][j]
-                ldsm_x4_trans(a, u.dh2b + (sr + lr_a) * SH_STRIDE + wid * 16 + lc_a);
-#pragma unroll
-                for (int np = 0; np < 4; np++) {
-                    uint32_t b[4];  // B[k = sample][n = i] = h1[sample][i]
-                    ldsm_x4_trans(b, u.m.h1 + (sr + lr_b) * SH_STRIDE + np * 16 + lc_b);
-                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
-                    mma_bf16_16816(a2[2 * np], a, b0);
-                    mma_bf16_16816(a2[2 * np + 1], a, b1);
-                }
-                // A[m = i][k = sample] = dH1[sample][i]
-                ldsm_x4_trans(a, u.dh1b + (sr + lr_a) * SH_STRIDE + wid * 16 + lc_a);
-#pragma unroll
-                for (int np = 0; np < 2; np++) {
-                    uint32_t b[4];  // B[k = sample][n = input] = x[sample][input]
-                    ldsm_x4_trans(b, u.m.x + (sr + lr_b) * SX_STRIDE + np * 16 + lc_b);
-                    const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
-                    mma_bf16_16816(a1[2 * np], a, b0);
-                    mma_bf16_16816(a1[2 * np + 1], a, b1);
-                }
-            }
-            const int j0 = wid * 16 + g, j1 = j0 + 8;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const int c0 = nt * 8 + 2 * t;
-                sG[MLP_OFF_W2 + j0 * MLP_H + c0] += a2[nt][0];
-                sG[MLP_OFF_W2 + j0 * MLP_H + c0 + 1] += a2[nt][1];
-                sG[MLP_OFF_W2 + j1 * MLP_H + c0] += a2[nt][2];
-                sG[MLP_OFF_W2 + j1 * MLP_H + c0 + 1] += a2[nt][3];
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const int f0 = nt * 8 + 2 * t;
-                if (f0 < MLP_IN) {
-                    sG[MLP_OFF_W1 + j0 * MLP_IN + f0] += a1[nt][0];
-                    sG[MLP_OFF_W1 + j1 * MLP_IN + f0] += a1[nt][2];
-                }
-                if (f0 + 1 < MLP_IN) {
-                    sG[MLP_OFF_W1 + j0 * MLP_IN + f0 + 1] += a1[nt][1];
-                    sG[MLP_OFF_W1 + j1 * MLP_IN + f0 + 1] += a1[nt][3];
-                }
-            }
-        }
-        // db1, db2, dw3, db3: FP32 sums over the 128 samples, one owner each
-        for (int q = threadIdx.x; q < 3 * MLP_H + 1; q += blockDim.x) {
-            float acc = 0.f;
-            for (int w = 0; w < TRAIN_WARPS; w++) {
-                const TrainSmemWarp &u = sWarp[w];
-                for (int r = 0; r < 32; r++) {
-                    if (q < MLP_H) acc = acc + u.dh1[r * HROW + q];
-                    else if (q < 2 * MLP_H) acc = acc + u.dh2[r * HROW + q - MLP_H];
-                    else if (q < 3 * MLP_H) acc = acc + u.dy[r] * u.h2[r * HROW + q - 2 * MLP_H];
-                    else acc = acc + u.dy[r];
-                }
-            }
-            const int p = q < MLP_H ? MLP_OFF_B1 + q
-                        : q < 2 * MLP_H ? MLP_OFF_B2 + q - MLP_H
-                        : q < 3 * MLP_H ? MLP_OFF_W3 + q - 2 * MLP_H
-                                        : MLP_OFF_B3;
-            sG[p] = sG[p] + acc;
-        }
-        __syncthreads();
+    for (int u = 0; u < 4; u++) {
+        const int k = (g + u) & 3;  // row r0 + k: 16 k bytes further in the core matrix
+        const uint32_t w = (k & 2) ? w23 : w01;
+        st_b16(tile, off + 16 * k, (k & 1) ? w >> 16 : w);
     }
-    for (int i = threadIdx.x; i < NGRAD; i += blockDim.x) partial[(long)blockIdx.x * NGRAD + i] = sG[i];
 }
 
-__global__ void grad_reduce_kernel(const float *partial, int nblocks, float *grad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= NGRAD) return;
+template <bool TRAIN>
+__global__ void __launch_bounds__(128, 1) mlp_tc_kernel(const MlpDev mlp, const float *X,
+                                                     const float *Z, long n, float *out,
+                                                     int *err) {
+    using namespace net;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr uint32_t NCOLS = TRAIN ? 256 : 128;
+    uint8_t *sA = smem + OFF_A, *sGA = smem + OFF_GA, *sGB = smem + OFF_GB;
+    uint8_t *sHA = smem + OFF_HA, *sDY = smem + OFF_DY;
+    float *sb1 = reinterpret_cast<float *>(smem + OFF_F), *sb2 = sb1 + MLP_H, *sw3 = sb2 + MLP_H;
+    float *sloss = sw3 + MLP_H + 1;  // after b3: one sum per warp
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + OFF_F + 800);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + OFF_F + 808);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+
+    // the first tile's inputs are loaded before the weights are staged, every
+    // later tile's while the MMAs of the one before run
+    float x[MLP_IN], zn = 0.f;
+    auto load_inputs = [&](long b) {
+        const long s = b + t;
+        const bool v = s < n;
+#pragma unroll
+        for (int i = 0; i < MLP_IN; i++) x[i] = v ? X[s * MLP_IN + i] : 0.f;
+        if (TRAIN) zn = v ? Z[s] : 0.f;
+    };
+    load_inputs((long)blockIdx.x * 128);
+    // the weights in 16-byte pieces (8 BF16 of a row), all loads issued first:
+    // W1 2 pieces per thread, W2 4 and, for training, W2^T 4
+    {
+        const uint4 *w1v = reinterpret_cast<const uint4 *>(mlp.w1);
+        const uint4 *w2v = reinterpret_cast<const uint4 *>(mlp.w2);
+        const uint4 *w2tv = reinterpret_cast<const uint4 *>(mlp.w2t);
+        uint4 p1[2], p2[4], p3[4];
+#pragma unroll
+        for (int u = 0; u < 2; u++) p1[u] = w1v[t + 128 * u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) p2[u] = w2v[t + 128 * u];
+        if (TRAIN) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) p3[u] = w2tv[t + 128 * u];
+        }
+        const float bv1 = t < MLP_H ? mlp.b1[t] : 0.f, bv2 = t < MLP_H ? mlp.b2[t] : 0.f;
+        const float wv3 = t < MLP_H ? mlp.w3[t] : 0.f, bv3 = mlp.b3[0];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int q = t + 128 * u;  // row q / 4, columns 8 (q % 4) ..
+            *reinterpret_cast<uint4 *>(smem + OFF_W1 +
+                                       kmajor_offset(q / 4, 8 * (q % 4), MLP_IN_PAD)) = p1[u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int q = t + 128 * u, j = q / 8, k0 = 8 * (q % 8);  // row j, columns k0 ..
+            *reinterpret_cast<uint4 *>(smem + OFF_W2 + kmajor_offset(j, k0, MLP_H)) = p2[u];
+            if (TRAIN)
+                *reinterpret_cast<uint4 *>(smem + OFF_W2T + kmajor_offset(j, k0, MLP_H)) = p3[u];
+        }
+        if (t < MLP_H) {
+            sb1[t] = bv1;
+            sb2[t] = bv2;
+            sw3[t] = wv3;
+        }
+        if (t == 0) sw3[MLP_H] = bv3;
+    }
+    if (TRAIN) {
+        // the constant rows: ones (bias gradients) and zeros (padding)
+        constexpr uint32_t ONE = 0x3F80u;  // 1.0 in BF16
+        for (int r = ROW_ONES; r < 96; r++) st_b16(sGB, kmajor_offset(r, t, 128), r == ROW_ONES ? ONE : 0u);
+        for (int r = MLP_H; r < 128; r++) st_b16(sHA, kmajor_offset(r, t, 128), r == MLP_H ? ONE : 0u);
+        for (int r = 1; r < 16; r++) st_b16(sDY, kmajor_offset(r, t, 128), 0u);
+        if (t < 4) sloss[t] = 0.f;
+    }
+    if (t == 0) mbar_init(mbar, 1);
+    if (warp == 0) tc_alloc(tslot, NCOLS);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t a_addr = smem_u32(sA), w1_addr = smem_u32(smem + OFF_W1);
+    const uint32_t w2_addr = smem_u32(smem + OFF_W2), w2t_addr = smem_u32(smem + OFF_W2T);
+    const uint32_t ga_addr = smem_u32(sGA), gb_addr = smem_u32(sGB);
+    const uint32_t ha_addr = smem_u32(sHA), dy_addr = smem_u32(sDY);
+    constexpr uint32_t ID64 = tc_idesc_bf16(128, MLP_H), ID96 = tc_idesc_bf16(128, 96),
+                       ID16 = tc_idesc_bf16(128, 16);
+    uint32_t phase = 0;
+    bool ok = true;
+    // every thread's shared-memory writes are made visible to the tensor core,
+    // thread 0 issues the MMAs and waits (bounded) for their commit while the
+    // others wait at the block barrier
+    auto run_mma = [&](auto issue) -> bool {
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+            issue();
+            tc_commit(mbar);
+        }
+        const bool done = __syncthreads_and(t == 0 ? mbar_wait(mbar, phase, TC_WAIT) : true);
+        phase ^= 1;
+        tc_fence_after();
+        return done;
+    };
+
+    const float inv_n = 1.f / (float)n;
+    int ntile = 0;
+    for (long base = (long)blockIdx.x * 128; base < n; base += (long)gridDim.x * 128, ntile++) {
+        const long s = base + t;
+        const bool valid = s < n;
+        const float zv = zn;
+        // 1. x -> row t of A (K 32); training: column t of X^T
+#pragma unroll
+        for (int h = 0; h < MLP_IN_PAD / 8; h++) {
+            uint32_t p[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int k0 = 8 * h + 2 * j;
+                p[j] = bf16x2_bits(k0 < MLP_IN ? x[k0] : 0.f, k0 + 1 < MLP_IN ? x[k0 + 1] : 0.f);
+            }
+            // rows 64 + k of [H1^T; X^T; 1; 0]: features 0-18, then the row of ones
+            constexpr uint32_t ONE_HI = 0x3F800000u;  // BF16 1.0 in the high half
+            static_assert(MLP_IN % 4 == 3, "the row of ones closes the features' last group of 4");
+            if (TRAIN && 8 * h < MLP_IN)
+                st_col4(sGB, MLP_H + 8 * h, t, p[0], 8 * h + 3 == MLP_IN ? p[1] | ONE_HI : p[1]);
+            if (TRAIN && 8 * h + 4 < MLP_IN)
+                st_col4(sGB, MLP_H + 8 * h + 4, t, p[2], 8 * h + 7 == MLP_IN ? p[3] | ONE_HI : p[3]);
+            *reinterpret_cast<uint4 *>(sA + kmajor_offset(t, 8 * h, MLP_IN_PAD)) =
+                make_uint4(p[0], p[1], p[2], p[3]);
+        }
+        if (base + (long)gridDim.x * 128 < n) load_inputs(base + (long)gridDim.x * 128);
+        ok = run_mma([&] {
+#pragma unroll
+            for (int k = 0; k < MLP_IN_PAD / 16; k++)
+                tc_mma_bf16(tmem + COL_H1, tc_desc(a_addr + 256 * k, 128, MLP_IN_PAD / 8 * 128),
+                            tc_desc(w1_addr + 256 * k, 128, MLP_IN_PAD / 8 * 128), ID64, k > 0);
+        });
+        if (!ok) break;
+        // 2. h1 = ReLU(D + b1) as BF16 -> row t of A (K 64); training: column t
+        // of H1^T and the mask h1 > 0
+        uint64_t m1 = 0;
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + COL_H1 + (uint32_t)c, v);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                uint32_t p[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int q = 8 * h + 2 * j;
+                    const float2 hv = __fadd2_rn(make_float2(v[q], v[q + 1]),
+                                                 make_float2(sb1[c + q], sb1[c + q + 1]));
+                    p[j] = bf16x2_relu(hv.x, hv.y);
+                    if (TRAIN) {
+                        m1 |= (uint64_t)((p[j] & 0xFFFFu) != 0u) << (c + q);
+                        m1 |= (uint64_t)((p[j] >> 16) != 0u) << (c + q + 1);
+                    }
+                }
+                if (TRAIN) {
+                    st_col4(sGB, c + 8 * h, t, p[0], p[1]);
+                    st_col4(sGB, c + 8 * h + 4, t, p[2], p[3]);
+                }
+                *reinterpret_cast<uint4 *>(sA + kmajor_offset(t, c + 8 * h, MLP_H)) =
+                    make_uint4(p[0], p[1], p[2], p[3]);
+            }
+        }
+        ok = run_mma([&] {
+#pragma unroll
+            for (int k = 0; k < MLP_H / 16; k++)
+                tc_mma_bf16(tmem + COL_H2, tc_desc(a_addr + 256 * k, 128, MLP_H / 8 * 128),
+                            tc_desc(w2_addr + 256 * k, 128, MLP_H / 8 * 128), ID64, k > 0);
+        });
+        if (!ok) break;
+        // 3. y = b3 + sum_j w3_j ReLU(D_j + b2_j), even and odd j in the two
+        // lanes of paired FP32 instructions
+        float2 y2 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + COL_H2 + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                float2 h = __fadd2_rn(make_float2(v[j], v[j + 1]),
+                                      make_float2(sb2[c + j], sb2[c + j + 1]));
+                h.x = fmaxf(h.x, 0.f);
+                h.y = fmaxf(h.y, 0.f);
+                y2 = __ffma2_rn(make_float2(sw3[c + j], sw3[c + j + 1]), h, y2);
+            }
+        }
+        const float yv = (y2.x + y2.y) + sw3[MLP_H];
+        if (!TRAIN) {
+            if (valid) out[s] = yv;
+            continue;
+        }
+        const float e = valid ? yv - zv : 0.f;
+        const float dy = 2.f * e * inv_n;
+        float e2 = e * e;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, d);
+        if (lane == 0) sloss[warp] += e2;
+        st_b16(sDY, kmajor_offset(0, t, 128), bf16x2_bits(dy, 0.f));
+        // dH2 = dy w3 (h2 > 0) as BF16 -> row t of A and column t of dH2^T;
+        // h2 as BF16 -> column t of H2^T
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + COL_H2 + (uint32_t)c, v);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                uint32_t p[4], hb[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int q = 8 * h + 2 * j;
+                    float2 hv = __fadd2_rn(make_float2(v[q], v[q + 1]),
+                                           make_float2(sb2[c + q], sb2[c + q + 1]));
+                    hv.x = fmaxf(hv.x, 0.f);
+                    hv.y = fmaxf(hv.y, 0.f);
+                    p[j] = bf16x2_bits(hv.x > 0.f ? dy * sw3[c + q] : 0.f,
+                                       hv.y > 0.f ? dy * sw3[c + q + 1] : 0.f);
+                    hb[j] = bf16x2_bits(hv.x, hv.y);
+                }
+                st_col4(sGA, c + 8 * h, t, p[0], p[1]);
+                st_col4(sGA, c + 8 * h + 4, t, p[2], p[3]);
+                st_col4(sHA, c + 8 * h, t, hb[0], hb[1]);
+                st_col4(sHA, c + 8 * h + 4, t, hb[2], hb[3]);
+                *reinterpret_cast<uint4 *>(sA + kmajor_offset(t, c + 8 * h, MLP_H)) =
+                    make_uint4(p[0], p[1], p[2], p[3]);
+            }
+        }
+        ok = run_mma([&] {
+#pragma unroll
+            for (int k = 0; k < MLP_H / 16; k++)
+                tc_mma_bf16(tmem + COL_H1, tc_desc(a_addr + 256 * k, 128, MLP_H / 8 * 128),
+                            tc_desc(w2t_addr + 256 * k, 128, MLP_H / 8 * 128), ID64, k > 0);
+        });
+        if (!ok) break;
+        // 4. dH1 = D (h1 > 0) as BF16 -> column t of dH1^T
+#pragma unroll
+        for (int c = 0; c < MLP_H; c += 32) {
+            float v[32];
+            tc_ld32(lane_base + COL_H1 + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+                const uint32_t p01 = bf16x2_bits((m1 >> (c + j)) & 1 ? v[j] : 0.f,
+                                                 (m1 >> (c + j + 1)) & 1 ? v[j + 1] : 0.f);
+                const uint32_t p23 = bf16x2_bits((m1 >> (c + j + 2)) & 1 ? v[j + 2] : 0.f,
+                                                 (m1 >> (c + j + 3)) & 1 ? v[j + 3] : 0.f);
+                st_col4(sGA, MLP_H + c + j, t, p01, p23);
+            }
+        }
+        const uint32_t acc = ntile > 0 ? 1u : 0u;
+        ok = run_mma([&] {
+#pragma unroll
+            for (int k = 0; k < 128 / 16; k++)
+                tc_mma_bf16(tmem + COL_G, tc_desc(ga_addr + 256 * k, 128, 128 / 8 * 128),
+                            tc_desc(gb_addr + 256 * k, 128, 128 / 8 * 128), ID96, acc | (k > 0));
+#pragma unroll
+            for (int k = 0; k < 128 / 16; k++)
+                tc_mma_bf16(tmem + COL_G3, tc_desc(ha_addr + 256 * k, 128, 128 / 8 * 128),
+                            tc_desc(dy_addr + 256 * k, 128, 128 / 8 * 128), ID16, acc | (k > 0));
+        });
+        if (!ok) break;
+    }
+    if (TRAIN && ok) {
+        // the block's sums: warps 0-1 hold rows j of dW2, db2 and dw3, warps
+        // 2-3 rows i of dW1 and db1, lane 64 db3
+        float *pb = out + (long)blockIdx.x * NGRAD;
+        float v[32];
+        if (ntile == 0) {
+            for (int i = t; i < NGRAD; i += 128) pb[i] = 0.f;
+        } else {
+            if (warp < 2) {
+#pragma unroll
+                for (int c = 0; c < MLP_H; c += 32) {
+                    tc_ld32(lane_base + COL_G + (uint32_t)c, v);
+#pragma unroll
+                    for (int i = 0; i < 32; i++) pb[MLP_OFF_W2 + t * MLP_H + c + i] = v[i];
+                }
+            }
+            tc_ld32(lane_base + COL_G + MLP_H, v);
+            if (warp < 2) {
+                pb[MLP_OFF_B2 + t] = v[MLP_IN];
+            } else {
+#pragma unroll
+                for (int f = 0; f < MLP_IN; f++) pb[MLP_OFF_W1 + (t - MLP_H) * MLP_IN + f] = v[f];
+                pb[MLP_OFF_B1 + t - MLP_H] = v[MLP_IN];
+            }
+            tc_ld32(lane_base + COL_G3, v);
+            if (t < MLP_H) pb[MLP_OFF_W3 + t] = v[0];
+            else if (t == MLP_H) pb[MLP_OFF_B3] = v[0];
+            if (t == 0) pb[MLP_NPARAM] = ((sloss[0] + sloss[1]) + (sloss[2] + sloss[3])) * inv_n;
+        }
+    }
+    if (!ok) {
+        // an MMA did not complete: record it, give it one more bounded wait so
+        // that no MMA is writing the columns when they are released
+        if (t == 0 && err) atomicExch(err, 1);
+        mbar_wait(mbar, phase ^ 1, TC_WAIT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, NCOLS);
+    if (t == 0) mbar_inval(mbar);
+}
+
+// one Adam step of the FP32 master parameters (p == nullptr: none)
+struct AdamStep {
+    float *p = nullptr, *m1 = nullptr, *m2 = nullptr;
+    __nv_bfloat16 *w1b = nullptr, *w2b = nullptr;
+    float lr = 0.f, b1c = 1.f, b2c = 1.f;  // rate, bias corrections 1 - beta^step
+};
+
+// Sums of the block partials: a block of 256 threads takes 32 parameters, 8
+// threads per parameter each sum a run of consecutive partials (16 loads in
+// flight, additions in block order), and the runs' sums are added in run
+// order -- a fixed order for a given block count.  The loss also goes into
+// *loss_slot (a step's entry of a device-side loss log) when given.  With
+// ad.p, the parameter's thread then takes its Adam step and refreshes the
+// parameter's BF16 copies.
+constexpr int RED_PAR = 32, RED_RUNS = 8;
+__global__ void __launch_bounds__(RED_PAR * RED_RUNS)
+    grad_reduce_kernel(const float *partial, int nblocks, float *grad, float *loss_slot,
+                       const AdamStep ad) {
+    __shared__ float run_sum[RED_RUNS][RED_PAR];
+    const int pl = threadIdx.x % RED_PAR, run = threadIdx.x / RED_PAR;
+    const int i = blockIdx.x * RED_PAR + pl;
+    const int per = (nblocks + RED_RUNS - 1) / RED_RUNS;
+    const int b0 = min(run * per, nblocks), b1 = min(b0 + per, nblocks);
     float s = 0.f;
-    for (int b = 0; b < nblocks; b++) s = s + partial[(long)b * NGRAD + i];
+    if (i < NGRAD) {
+        int b = b0;
+        for (; b + 16 <= b1; b += 16) {
+            float v[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) v[u] = partial[(long)(b + u) * NGRAD + i];
+#pragma unroll
+            for (int u = 0; u < 16; u++) s = s + v[u];
+        }
+        for (; b < b1; b++) s = s + partial[(long)b * NGRAD + i];
+    }
+    run_sum[run][pl] = s;
+    __syncthreads();
+    if (run != 0 || i >= NGRAD) return;
+    s = run_sum[0][pl];
+#pragma unroll
+    for (int r = 1; r < RED_RUNS; r++) s = s + run_sum[r][pl];
     grad[i] = s;
-}
-
-// Adam step on the FP32 master parameters, refreshing the BF16 copies
-__global__ void adam_kernel(float *p, float *m1, float *m2, const float *grad, float lr,
-                            float b1c, float b2c, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= MLP_NPARAM) return;
-    const float gr = grad[i];
-    const float a = 0.9f * m1[i] + 0.1f * gr;
-    const float b = 0.999f * m2[i] + 0.001f * gr * gr;
-    m1[i] = a;
-    m2[i] = b;
-    const float v = p[i] - lr * (a / b1c) / (sqrtf(b / b2c) + 1e-8f);
-    p[i] = v;
-    if (i < MLP_OFF_B1) w1b[(i / MLP_IN) * MLP_IN_PAD + i % MLP_IN] = __float2bfloat16_rn(v);
-    else if (i >= MLP_OFF_W2 && i < MLP_OFF_B2) w2b[i - MLP_OFF_W2] = __float2bfloat16_rn(v);
+    if (i == MLP_NPARAM) {
+        if (loss_slot) *loss_slot = s;
+        return;
+    }
+    if (!ad.p) return;
+    const float a = 0.9f * ad.m1[i] + 0.1f * s;
+    const float q = 0.999f * ad.m2[i] + 0.001f * s * s;
+    ad.m1[i] = a;
+    ad.m2[i] = q;
+    const float v = ad.p[i] - ad.lr * (a / ad.b1c) / (sqrtf(q / ad.b2c) + 1e-8f);
+    ad.p[i] = v;
+    if (i < MLP_OFF_B1)
+        ad.w1b[(i / MLP_IN) * MLP_IN_PAD + i % MLP_IN] = __float2bfloat16_rn(v);
+    else if (i >= MLP_OFF_W2 && i < MLP_OFF_B2) {
+        const int e = i - MLP_OFF_W2;  // W2[e / 64][e % 64], then its transposed copy
+        ad.w2b[e] = __float2bfloat16_rn(v);
+        ad.w2b[MLP_H * MLP_H + (e % MLP_H) * MLP_H + e / MLP_H] = __float2bfloat16_rn(v);
+    }
 }
 
 __global__ void refresh_bf16_kernel(const float *p, __nv_bfloat16 *w1b, __nv_bfloat16 *w2b) {
@@ -793,27 +909,9 @@ __global__ void refresh_bf16_kernel(const float *p, __nv_bfloat16 *w1b, __nv_bfl
         const int j = i / MLP_IN_PAD, f = i % MLP_IN_PAD;
         w1b[i] = __float2bfloat16_rn(f < MLP_IN ? p[MLP_OFF_W1 + j * MLP_IN + f] : 0.f);
     }
-    if (i < MLP_H * MLP_H) w2b[i] = __float2bfloat16_rn(p[MLP_OFF_W2 + i]);
-}
-
-// inference of the network on rows of features (the closure kernel's forward)
-__global__ void __launch_bounds__(128) mlp_forward_kernel(MlpDev mlp, const float *X, long n,
-                                                          float *Y) {
-    __shared__ MlpSmemWeights sW;
-    __shared__ MlpSmemWarp sWarp[4];
-    mlp_load_weights(sW, mlp);
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    MlpSmemWarp &sw = sWarp[threadIdx.x >> 5];
-    for (long base = (long)blockIdx.x * 128; base < n; base += (long)gridDim.x * 128) {
-        const long s = base + threadIdx.x;
-        for (int i = 0; i < MLP_IN_PAD; i++)
-            sw.x[lane * SX_STRIDE + i] =
-                __float2bfloat16_rn((s < n && i < MLP_IN) ? X[s * MLP_IN + i] : 0.f);
-        float h2[2][8][4];
-        mlp_forward_warp(sW, sw, h2, true);
-        if (s < n) Y[s] = sw.y[lane];
-        __syncwarp();
+    if (i < MLP_H * MLP_H) {
+        w2b[i] = __float2bfloat16_rn(p[MLP_OFF_W2 + i]);
+        w2b[MLP_H * MLP_H + (i % MLP_H) * MLP_H + i / MLP_H] = w2b[i];
     }
 }
 
@@ -821,7 +919,8 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(MlpDev mlp, const floa
 
 struct lb_mlp {
     float *p = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *partial = nullptr;
-    __nv_bfloat16 *w1b = nullptr, *w2b = nullptr;
+    __nv_bfloat16 *w1b = nullptr, *w2b = nullptr;  // w2b: W2 [64][64], then W2^T
+    int *err_dev = nullptr;  // device word: a tensor-core MMA of the network never completed
     int nblocks = 304;
     long step = 0;
     cudaStream_t stream = nullptr;
@@ -834,6 +933,7 @@ MlpDev mlp_dev(const lb_mlp *m) {
     MlpDev d;
     d.w1 = m->w1b;
     d.w2 = m->w2b;
+    d.w2t = m->w2b + MLP_H * MLP_H;
     d.b1 = m->p + MLP_OFF_B1;
     d.b2 = m->p + MLP_OFF_B2;
     d.w3 = m->p + MLP_OFF_W3;
@@ -851,20 +951,43 @@ int mfail(lb_mlp *m, cudaError_t e, const char *where) {
         if (e_ != cudaSuccess) return mfail(m, e_, where);        \
     } while (0)
 
-int mlp_gradient(lb_mlp *m, const float *X, const float *Z, long n) {
-    static bool attr = false;
-    if (!attr) {
-        LB_MTRY(m, "cudaFuncSetAttribute",
-                cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)TRAIN_SMEM));
-        attr = true;
+// the network kernels' dynamic shared memory above the default 48 KB
+cudaError_t mlp_kernel_attributes() {
+    static cudaError_t done = cudaErrorNotReady;
+    if (done == cudaErrorNotReady) {
+        done = cudaFuncSetAttribute(mlp_tc_kernel<true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, net::TRAIN_SMEM);
+        if (done == cudaSuccess)
+            done = cudaFuncSetAttribute(mlp_tc_kernel<false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, NET_FWD_SMEM);
     }
+    return done;
+}
+
+// the kernels' error word: nonzero when an MMA never completed
+int mlp_check(lb_mlp *m) {
+    int h = 0;
+    LB_MTRY(m, "mlp error word", cudaMemcpyAsync(&h, m->err_dev, sizeof(int),
+                                                 cudaMemcpyDeviceToHost, m->stream));
+    LB_MTRY(m, "mlp error word", cudaStreamSynchronize(m->stream));
+    if (h) {
+        m->err = "a tensor-core MMA of the network did not complete (bounded wait ran out)";
+        return LB_ERR_CUDA;
+    }
+    return LB_OK;
+}
+
+// the gradient over n samples into m->grad, then (ad.p) the Adam step
+int mlp_gradient(lb_mlp *m, const float *X, const float *Z, long n, float *loss_slot = nullptr,
+                 const AdamStep &ad = AdamStep()) {
+    LB_MTRY(m, "cudaFuncSetAttribute", mlp_kernel_attributes());
     const long chunks = (n + 127) / 128;
     const int nb = (int)std::min<long>(m->nblocks, chunks);
-    mlp_train_kernel<<<nb, 32 * TRAIN_WARPS, TRAIN_SMEM, m->stream>>>(mlp_dev(m), X, Z, n,
-                                                                      m->partial);
-    LB_MTRY(m, "mlp_train_kernel", cudaGetLastError());
-    grad_reduce_kernel<<<(NGRAD + 255) / 256, 256, 0, m->stream>>>(m->partial, nb, m->grad);
+    mlp_tc_kernel<true><<<nb, 128, net::TRAIN_SMEM, m->stream>>>(mlp_dev(m), X, Z, n, m->partial,
+                                                                 m->err_dev);
+    LB_MTRY(m, "mlp_tc_kernel", cudaGetLastError());
+    grad_reduce_kernel<<<(NGRAD + RED_PAR - 1) / RED_PAR, RED_PAR * RED_RUNS, 0, m->stream>>>(
+        m->partial, nb, m->grad, loss_slot, ad);
     LB_MTRY(m, "grad_reduce_kernel", cudaGetLastError());
     return LB_OK;
 }
@@ -883,7 +1006,9 @@ int lb_mlp_create(uint64_t seed, lb_mlp **out) {
     if (e == cudaSuccess) e = cudaMalloc(&m->grad, sizeof(float) * NGRAD);
     if (e == cudaSuccess) e = cudaMalloc(&m->partial, sizeof(float) * NGRAD * m->nblocks);
     if (e == cudaSuccess) e = cudaMalloc(&m->w1b, sizeof(__nv_bfloat16) * MLP_H * MLP_IN_PAD);
-    if (e == cudaSuccess) e = cudaMalloc(&m->w2b, sizeof(__nv_bfloat16) * MLP_H * MLP_H);
+    if (e == cudaSuccess) e = cudaMalloc(&m->w2b, sizeof(__nv_bfloat16) * 2 * MLP_H * MLP_H);
+    if (e == cudaSuccess) e = cudaMalloc(&m->err_dev, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(m->err_dev, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         lb_mlp_destroy(m);
@@ -913,7 +1038,7 @@ int lb_mlp_destroy(lb_mlp *m) {
     if (!m) return LB_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->p); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad); cudaFree(m->partial);
-    cudaFree(m->w1b); cudaFree(m->w2b);
+    cudaFree(m->w1b); cudaFree(m->w2b); cudaFree(m->err_dev);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return LB_OK;
@@ -945,11 +1070,20 @@ int lb_mlp_get_params(lb_mlp *m, float *p) {
 
 int lb_mlp_forward(lb_mlp *m, const float *x_dev, float *y_dev, long n) {
     if (!m || !x_dev || !y_dev || n < 0) return LB_ERR_ARG;
-    const int nb = (int)std::min<long>(1216, (n + 127) / 128);
-    if (nb > 0) mlp_forward_kernel<<<nb, 128, 0, m->stream>>>(mlp_dev(m), x_dev, n, y_dev);
-    LB_MTRY(m, "mlp_forward_kernel", cudaGetLastError());
-    LB_MTRY(m, "mlp_forward", cudaStreamSynchronize(m->stream));
-    return LB_OK;
+    LB_MTRY(m, "cudaFuncSetAttribute", mlp_kernel_attributes());
+    static int cap = 0;  // SMs x 4: the blocks whose tensor memory (128 columns) fits at once
+    if (!cap) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cap = 4 * sms;
+    }
+    const int nb = (int)std::min<long>(cap, (n + 127) / 128);
+    if (nb > 0)
+        mlp_tc_kernel<false><<<nb, 128, NET_FWD_SMEM, m->stream>>>(mlp_dev(m), x_dev, nullptr, n,
+                                                                   y_dev, m->err_dev);
+    LB_MTRY(m, "mlp_tc_kernel", cudaGetLastError());
+    return mlp_check(m);
 }
 
 int lb_mlp_grad(lb_mlp *m, const float *x_dev, const float *z_dev, long n, float *grad,
@@ -960,39 +1094,50 @@ int lb_mlp_grad(lb_mlp *m, const float *x_dev, const float *z_dev, long n, float
     std::vector<float> h(NGRAD);
     LB_MTRY(m, "grad", cudaMemcpyAsync(h.data(), m->grad, sizeof(float) * NGRAD,
                                        cudaMemcpyDeviceToHost, m->stream));
-    LB_MTRY(m, "grad", cudaStreamSynchronize(m->stream));
+    const int crc = mlp_check(m);
+    if (crc != LB_OK) return crc;
     if (grad) memcpy(grad, h.data(), sizeof(float) * MLP_NPARAM);
     if (loss) *loss = h[MLP_NPARAM];
     return LB_OK;
 }
 
 // Adam over random contiguous windows of `batch` samples (a 64-bit LCG
-// picks the window starts); loss_log[i] = loss of step i (optional)
+// picks the window starts); loss_log[i] = loss of step i (optional).  The
+// steps are queued without a host round trip: the losses go to a device log
+// that is copied back once.
 int lb_mlp_train(lb_mlp *m, const float *x_dev, const float *z_dev, long n, int steps,
                  int batch, float lr, uint64_t seed, float *loss_log) {
     if (!m || !x_dev || !z_dev || n < 1 || steps < 0 || batch < 1) return LB_ERR_ARG;
     if (batch > n) batch = (int)n;
+    float *log_dev = nullptr;
+    if (loss_log && steps > 0)
+        LB_MTRY(m, "loss log", cudaMalloc(&log_dev, sizeof(float) * steps));
+    struct Free {
+        float *p;
+        ~Free() { cudaFree(p); }
+    } free_log{log_dev};
     uint64_t st = seed * 2862933555777941757ULL + 3037000493ULL;
     for (int it = 0; it < steps; it++) {
         st = st * 6364136223846793005ULL + 1442695040888963407ULL;
         const long start = (long)((st >> 17) % (uint64_t)(n - batch + 1));
-        int rc = mlp_gradient(m, x_dev + start * MLP_IN, z_dev + start, batch);
-        if (rc != LB_OK) return rc;
         m->step++;
-        const float b1c = 1.f - powf(0.9f, (float)m->step), b2c = 1.f - powf(0.999f, (float)m->step);
-        adam_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, m->stream>>>(m->p, m->m1, m->m2, m->grad,
-                                                                     lr, b1c, b2c, m->w1b, m->w2b);
-        LB_MTRY(m, "adam_kernel", cudaGetLastError());
-        if (loss_log) {
-            float l;
-            LB_MTRY(m, "loss", cudaMemcpyAsync(&l, m->grad + MLP_NPARAM, sizeof(float),
-                                               cudaMemcpyDeviceToHost, m->stream));
-            LB_MTRY(m, "loss", cudaStreamSynchronize(m->stream));
-            loss_log[it] = l;
-        }
+        AdamStep ad;
+        ad.p = m->p;
+        ad.m1 = m->m1;
+        ad.m2 = m->m2;
+        ad.w1b = m->w1b;
+        ad.w2b = m->w2b;
+        ad.lr = lr;
+        ad.b1c = 1.f - powf(0.9f, (float)m->step);
+        ad.b2c = 1.f - powf(0.999f, (float)m->step);
+        const int rc = mlp_gradient(m, x_dev + start * MLP_IN, z_dev + start, batch,
+                                    log_dev ? log_dev + it : nullptr, ad);
+        if (rc != LB_OK) return rc;
     }
-    LB_MTRY(m, "train", cudaStreamSynchronize(m->stream));
-    return LB_OK;
+    if (log_dev)
+        LB_MTRY(m, "loss log", cudaMemcpyAsync(loss_log, log_dev, sizeof(float) * steps,
+                                               cudaMemcpyDeviceToHost, m->stream));
+    return mlp_check(m);
 }
 
 int lb_closure_enable(lb_ctx *ctx, const lb_mlp *m, float nu0, float s_ref, float z_max,

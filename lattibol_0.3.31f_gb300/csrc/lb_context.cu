@@ -30,11 +30,11 @@ struct lb_ctx {
     float *sc = nullptr;                 // psi (D3Q19, D2Q9) and ueq_x, ueq_y (D2Q9)
     float *stage = nullptr;              // 16-bit storage: one float array for conversions
     double *red = nullptr;               // reduction partials + result
-    int *psync = nullptr;                // D2Q9 persistent loop: error word + band step counts
+    int *errw = nullptr;                 // device error word of the kernels that wait on the GPU
     float4 *probe_host = nullptr;        // lb_run_probe: mapped page-locked cursor value
     float4 *probe_dev = nullptr;         // its device address
     int probe_o = -1;                    // cursor node the captured graphs write (-1: none)
-    bool persist_pending = false;        // a persistent launch whose error word is unread
+    bool err_pending = false;            // a launch whose error word is unread
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps starting from set 0 / 1
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -88,9 +88,7 @@ int cuda_fail(lb_ctx *c, const char *where, cudaError_t e) {
 // launch tuning used when the caller leaves lb_config.tuning at LB_TUNE_DEFAULT.
 // D3Q19: the alternating sweep measured 44.7 vs 43.8 GLUPS on the 256x128x128
 // channel.  D2Q9: programmatic dependent launches measured 24.9 vs 22.7 GLUPS
-// on the 256^2 cavity (the alternating sweep: 23.8 with them); the persistent
-// loop measured 9.7 (each step waits on a chain of L2 round trips) and stays
-// opt-in.  Temporal blocks of 5 steps on 32x14 tiles (native mode without
+// on the 256^2 cavity (the alternating sweep: 23.8 with them).  Temporal blocks of 5 steps on 32x14 tiles (native mode without
 // Shan-Chen) measured 48.5 vs 24.1 GLUPS at 256^2, 11.1 vs 5.8 at 128^2 and
 // 73.3 vs 60.9 at 512^2, but 94.7 vs 101.5 at 1024^2 (a step then streams
 // from L2 faster than the blocks recompute their halos), so they are the
@@ -161,12 +159,6 @@ bool sc_stage_on(const lb_ctx *c) {
            19L * c->stride < (1L << 32);
 }
 
-// the D2Q9 persistent step loop applies: no Shan-Chen pass and the tuning
-// asks for it
-bool persistent_on(const lb_ctx *c) {
-    return c->Q == 9 && !sc_on(c) && (c->tune & LB_TUNE_PERSISTENT);
-}
-
 // the temporal-blocking shape in effect (0 = per-step launches): D2Q9 native
 // mode without Shan-Chen, and the tuning asks for it
 int tblock_variant(const lb_ctx *c) {
@@ -204,18 +196,18 @@ cudaError_t slab_join(lb_ctx *c) {
 }
 
 // after the stream has been synchronised: the device error word written by
-// the kernels that wait on the GPU (a persistent D2Q9 block that gave up
-// waiting for a neighbour band; a tcgen05 closure MMA that never completed)
-int check_persistent(lb_ctx *c) {
-    if (!c->persist_pending) return LB_OK;
+// the kernels that wait on the GPU (a tcgen05 closure MMA that never
+// completed; a staged Shan-Chen block whose copies never arrived)
+int check_device_error(lb_ctx *c) {
+    if (!c->err_pending) return LB_OK;
     int word = 0;
     LB_TRY(c, "device error word",
-           cudaMemcpy(&word, c->psync, sizeof(int), cudaMemcpyDeviceToHost));
-    c->persist_pending = false;
+           cudaMemcpy(&word, c->errw, sizeof(int), cudaMemcpyDeviceToHost));
+    c->err_pending = false;
     if (word != 0) {
-        LB_TRY(c, "device error word", cudaMemset(c->psync, 0, sizeof(int)));
+        LB_TRY(c, "device error word", cudaMemset(c->errw, 0, sizeof(int)));
         return fail(c, LB_ERR_DEVICE,
-                    "a kernel gave up waiting on the GPU (persistent band or tensor-core MMA)");
+                    "a kernel gave up waiting on the GPU (tensor-core MMA or staged copies)");
     }
     return LB_OK;
 }
@@ -283,16 +275,15 @@ cudaError_t step_once(lb_ctx *c, int from, bool moments) {
         if (c->closure_on) {
             c->launches += 1;
             ClosureArgs ca = c->closure;
-            ca.err = c->psync;
-            ca.legacy_mma = (c->tune & LB_TUNE_CLOSURE_MMA_SYNC) ? 1 : 0;
-            c->persist_pending = true;  // the tcgen05 kernel reports through psync[0]
+            ca.err = c->errw;
+            c->err_pending = true;  // the tcgen05 kernel reports through the error word
             return launch_d3q19_closure(a, ca, moments, c->stream);
         }
         const bool sc = sc_on(c);
         if (sc_stage_on(c)) {
             c->launches += 1;
-            a.err = c->psync;
-            c->persist_pending = true;  // a block that gave up waiting reports through psync[0]
+            a.err = c->errw;
+            c->err_pending = true;  // a block that gave up waiting reports through the error word
             // TMA copies for the 16-bit storage forms (42.0 vs 39.3 GLUPS at 256^3
             // against the same layout by cp.async); FP32 keeps the compact
             // cp.async stages (TMA measured 27.1 against 32.6 and 34.9 compact)
@@ -442,7 +433,7 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
     if (!(c->cfg.rho_ref > 0.f)) c->cfg.rho_ref = 1.f;
     c->tune = (cfg->tuning & LB_TUNE_EXPLICIT)
-                  ? (cfg->tuning & 0x1f0ff)
+                  ? (cfg->tuning & 0x1f0eb)
                   : (cfg->lattice == LB_D2Q9 ? LB_TUNE_LIBRARY_DEFAULT_D2
                                              : LB_TUNE_LIBRARY_DEFAULT_D3);
     if (!(cfg->tuning & LB_TUNE_EXPLICIT) && cfg->lattice == LB_D2Q9 &&
@@ -468,8 +459,8 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     // reduction partials, 7 results, then 4 floats (2 doubles) for lb_probe
     if (e == cudaSuccess) e = cudaMalloc(&c->red, sizeof(double) * (reduce_partials_size() + 16));
     if (e == cudaSuccess)
-        e = cudaMalloc(&c->psync, sizeof(int) * (c->Q == 9 ? cfg->ny + 1 : 1));
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->psync, 0, sizeof(int), c->stream);
+        e = cudaMalloc(&c->errw, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->errw, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -500,7 +491,7 @@ int lb_destroy(lb_ctx *c) {
     if (c->sc) cudaFree(c->sc);
     if (c->stage) cudaFree(c->stage);
     if (c->red) cudaFree(c->red);
-    if (c->psync) cudaFree(c->psync);
+    if (c->errw) cudaFree(c->errw);
     if (c->probe_host) cudaFreeHost(c->probe_host);
     if (c->side) cudaStreamSynchronize(c->side);
     for (int i = 0; i < 2; i++)
@@ -576,7 +567,7 @@ int lb_get_populations(lb_ctx *c, float *f) {
         // the staging array is reused by the next population
         LB_TRY(c, "lb_get_populations", cudaStreamSynchronize(c->stream));
     }
-    return check_persistent(c);
+    return check_device_error(c);
 }
 
 int lb_init_equilibrium(lb_ctx *c, const float *rho, const float *ux, const float *uy,
@@ -621,26 +612,6 @@ int lb_step(lb_ctx *c, int nsteps) {
         return fail(c, LB_ERR_STATE, "lb_step: a slab steps with lb_slab_step or "
                                      "lb_slab_group_step (its ghost planes need the exchange)");
     if (nsteps == 0) return LB_OK;
-    if (persistent_on(c)) {
-        // every step in one cooperative launch; falls through to the graphs
-        // when the bands cannot all be resident
-        LB_TRY(c, "lb_step", cudaMemsetAsync(c->psync, 0, sizeof(int) * (c->cfg.ny + 1),
-                                             c->stream));
-        const cudaError_t e =
-            launch_d2q9_persistent(d2_args(c, c->cur),
-                                   c->cfg.mode == LB_MODE_REFERENCE ? MODE_REF : MODE_NATIVE,
-                                   nsteps, c->psync, c->stream);
-        if (e == cudaSuccess) {
-            c->launches += 1;
-            c->persist_pending = true;
-            c->cur = (c->cur + nsteps) & 1;
-            c->steps += nsteps;
-            return LB_OK;
-        }
-        if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported)
-            return cuda_fail(c, "lb_step (persistent)", e);
-        (void)cudaGetLastError();
-    }
     if (const int tv = tblock_variant(c)) {
         // temporal blocks of T steps (graphs of L blocks); the last block, or
         // the last per-step launch of a remainder, writes the moments
@@ -696,7 +667,7 @@ int lb_get_moments(lb_ctx *c, float *rho, float *ux, float *uy, float *uz) {
                                c->stream));
     }
     LB_TRY(c, "lb_get_moments", cudaStreamSynchronize(c->stream));
-    return check_persistent(c);
+    return check_device_error(c);
 }
 
 int lb_reduce(lb_ctx *c, double out[7]) {
@@ -713,7 +684,7 @@ int lb_reduce(lb_ctx *c, double out[7]) {
     c->launches += 2;
     LB_TRY(c, "lb_reduce", cudaMemcpyAsync(out, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
     LB_TRY(c, "lb_reduce", cudaStreamSynchronize(c->stream));
-    return check_persistent(c);
+    return check_device_error(c);
 }
 
 int lb_probe(lb_ctx *c, int x, int y, int z, float value[4]) {
@@ -758,7 +729,7 @@ int lb_run_probe(lb_ctx *c, int nsteps, int x, int y, int z, float value[4]) {
         int rc = lb_step(c, nsteps);
         if (rc != LB_OK) return rc;
         LB_TRY(c, "lb_run_probe", cudaStreamSynchronize(c->stream));
-        rc = check_persistent(c);
+        rc = check_device_error(c);
         if (rc != LB_OK) return rc;
         memcpy(value, (const void *)c->probe_host, 4 * sizeof(float));
         return LB_OK;
@@ -794,7 +765,7 @@ int lb_synchronize(lb_ctx *c) {
     if (!c) return LB_ERR_ARG;
     LB_TRY(c, "lb_synchronize", slab_join(c));
     LB_TRY(c, "lb_synchronize", cudaStreamSynchronize(c->stream));
-    return check_persistent(c);
+    return check_device_error(c);
 }
 
 int lb_time_steps(lb_ctx *c, int nsteps, float *ms) {
@@ -805,7 +776,7 @@ int lb_time_steps(lb_ctx *c, int nsteps, float *ms) {
     LB_TRY(c, "lb_time_steps", cudaEventRecord(c->ev1, c->stream));
     LB_TRY(c, "lb_time_steps", cudaEventSynchronize(c->ev1));
     LB_TRY(c, "lb_time_steps", cudaEventElapsedTime(ms, c->ev0, c->ev1));
-    return check_persistent(c);
+    return check_device_error(c);
 }
 
 int64_t lb_launch_count(const lb_ctx *c) { return c ? c->launches : -1; }

@@ -305,155 +305,6 @@ __global__ void d2q9_equilibrium_kernel(Pop<9> p, const float *rho, const float 
     for (int k = 0; k < 9; k++) p.f[k][o] = g[k];
 }
 
-// ---------------------------------------------------------------------------
-// Persistent step loop for small lattices, where one step costs less than a
-// kernel launch.  One cooperative launch runs every step of a batch: block b
-// owns rows [b*rows, b*rows + rows) and, after each step, publishes how many
-// steps it has finished and waits only for the two bands its next pulls read
-// (rows y-1 and y+1).  Waiting for them also protects the buffer it is about
-// to overwrite: they have finished reading it.  Each wait is bounded; a block
-// that gives up raises sync[0] and every block leaves at its next check.
-// Pulls bypass L1 (ld.global.cg): L1 does not see the other SMs' stores.  The
-// per-node arithmetic is d2q9_fused_kernel's, so results are the same bits.
-// ---------------------------------------------------------------------------
-template <int MODE>
-__device__ __forceinline__ void d2q9_node_l2(const D2Args &a, int par, int x, int y, bool mom) {
-    // par = 0: a.src -> a.dst; par = 1: the other way
-    const float *const *src =
-        par ? (const float *const *)a.dst.f : (const float *const *)a.src.f;
-    float *const *dst = par ? (float *const *)a.src.f : (float *const *)a.dst.f;
-    const int o = x + a.W * y;
-    const uint8_t fl = a.flags[o];
-    const Nbr2 n(x, y, a.W, a.H);
-    if (fl & CELL_WALL) {
-        if (MODE == MODE_REF) {
-            const bool sb_self = a.sb[o] != 0;
-#pragma unroll
-            for (int m = 0; m < 9; m++) {
-                float v;
-                if (m == 0) {
-                    v = __ldcg(src[0] + o);
-                } else {
-                    const int on = o + n.off(d2_cx(m), d2_cr(m));
-                    const bool resp_sb = d2_pos(m) ? sb_self : (a.sb[on] != 0);
-                    v = resp_sb ? __ldcg(src[m] + o) : __ldcg(src[d2_opp(m)] + on);
-                }
-                dst[m][o] = v;
-            }
-        }
-        if (mom) { a.ux[o] = 0.f; a.uy[o] = 0.f; a.rho[o] = 0.f; }
-        if (a.probe && o == a.probe_o) *a.probe = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
-    }
-    float g[9];
-    if (MODE == MODE_NATIVE && (fl & CELL_NEAR_WALL)) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-            const int up = o + n.off(-d2_cx(k), -d2_cr(k));
-            const uint8_t fu = k == 0 ? 0 : a.flags[up];
-            if (fu & CELL_WALL) {
-                const float v = __ldcg(src[d2_opp(k)] + o);
-                g[k] = (fu & CELL_MOVING) ? v - a.corr[d2_opp(k)] : v;
-            } else {
-                g[k] = __ldcg(src[k] + up);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 9; k++) g[k] = __ldcg(src[k] + o + n.off(-d2_cx(k), -d2_cr(k)));
-    }
-    if (MODE == MODE_REF) {
-        if (x == 0 && a.dev == 0)
-            d2q9_zou_he_west(g, a.ux_in);
-        else if (x == a.W - 1 && a.dev == a.ndev - 1)
-            d2q9_zou_he_east(g, a.rho_out);
-    }
-    float rho, ux, uy;
-    if (MODE == MODE_NATIVE) {
-        d2q9_collide_native(g, a.Fx, a.Fy, a.w0, a.w1, a.w5, a.tau_inv, rho, ux, uy);
-    } else {
-        d2q9_moments(g, rho, ux, uy);
-        float ex = ux, ey = uy;
-        if (a.Fx != 0.f) ex = ux + a.Fx / (rho * a.tau_inv);
-        if (a.Fy != 0.f) ey = uy + a.Fy / (rho * a.tau_inv);
-        d2q9_bgk(g, ex, ey, rho, a.w0, a.w1, a.w5, a.tau_inv);
-    }
-    if (mom) { a.ux[o] = ux; a.uy[o] = uy; a.rho[o] = rho; }
-    if (a.probe && o == a.probe_o) *a.probe = make_float4(ux, uy, 0.f, rho);
-#pragma unroll
-    for (int k = 0; k < 9; k++) dst[k][o] = g[k];
-}
-
-// sync[0]: error word; sync[1 + b]: steps finished by band b (zero at launch)
-template <int MODE>
-__global__ void __launch_bounds__(1024) d2q9_persistent_kernel(const D2Args a, int nsteps,
-                                                               int rows, int *sync) {
-    __shared__ int give_up;
-    const int nb = gridDim.x, b = blockIdx.x;
-    const int y0 = b * rows, y1 = min(y0 + rows, a.H);
-    const int nodes = (y1 - y0) * a.W;
-    for (int s = 0; s < nsteps; s++) {
-        const bool mom = s == nsteps - 1;  // the last step writes the moment fields
-        for (int i = threadIdx.x; i < nodes; i += blockDim.x)
-            d2q9_node_l2<MODE>(a, s & 1, i % a.W, y0 + i / a.W, mom);
-        if (s == nsteps - 1) break;
-        // the block's stores are ordered before thread 0's release by the
-        // barrier; the acquiring block's barrier extends the order to its threads
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            st_release_gpu(sync + 1 + b, s + 1);
-            bool ok = true;
-            if (nb > 1) {
-                ok = wait_band(sync + 1 + (b + nb - 1) % nb, s + 1, sync);
-                if (ok) ok = wait_band(sync + 1 + (b + 1) % nb, s + 1, sync);
-            }
-            give_up = ok ? 0 : 1;
-        }
-        __syncthreads();
-        if (give_up) return;
-    }
-}
-
-// self-check of the bounded wait: block 0 waits for a band counter that no
-// block raises; it must give up after `limit` polls and raise sync[0]
-__global__ void band_wait_selftest_kernel(int *sync, int limit) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) wait_band(sync + 1, 1, sync, limit);
-}
-
-cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s) {
-    band_wait_selftest_kernel<<<2, 32, 0, s>>>(sync, limit);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_d2q9_persistent(const D2Args &a, int mode, int nsteps, int *sync,
-                                   cudaStream_t s) {
-    if (nsteps <= 0) return cudaSuccess;
-    int dev = 0, sms = 0, coop = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-    if (e != cudaSuccess) return e;
-    if (!coop) return cudaErrorNotSupported;
-    void (*kern)(const D2Args, int, int, int *) =
-        mode == MODE_REF ? d2q9_persistent_kernel<MODE_REF> : d2q9_persistent_kernel<MODE_NATIVE>;
-    // the narrowest bands whose blocks all fit on the GPU at once
-    for (int rows = 1; rows <= a.H; rows *= 2) {
-        const int nb = (a.H + rows - 1) / rows;
-        const int threads = std::min(1024, (rows * a.W + 31) / 32 * 32);
-        int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
-        if (e != cudaSuccess) return e;
-        if ((long)per_sm * sms >= nb) {
-            D2Args args = a;
-            int n = nsteps, r = rows;
-            void *params[] = {&args, &n, &r, &sync};
-            return cudaLaunchCooperativeKernel((const void *)kern, dim3(nb), dim3(threads), params,
-                                               0, s);
-        }
-    }
-    return cudaErrorCooperativeLaunchTooLarge;
-}
-
 // ---------------------------------------------------------------- launchers
 static dim3 grid2(int W, int H) { return dim3((W + D2_BLOCK - 1) / D2_BLOCK, H); }
 

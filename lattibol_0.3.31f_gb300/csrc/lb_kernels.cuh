@@ -86,35 +86,6 @@ struct D2Args {
     int probe_o;
 };
 
-// ---- waits between blocks of one persistent launch (all blocks resident):
-// release/acquire at GPU scope, and a bounded spin that raises an error word
-// instead of waiting forever
-constexpr int PERSIST_SPIN_LIMIT = 1 << 22;
-
-__device__ __forceinline__ void st_release_gpu(int *p, int v) {
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// true once *flag >= target; false when this wait gave up (it then raises
-// *err) or another block already has
-__device__ __forceinline__ bool wait_band(const int *flag, int target, int *err,
-                                          int limit = PERSIST_SPIN_LIMIT) {
-    for (int i = 0; i < limit; i++) {
-        if (ld_acquire_gpu(flag) >= target) return true;
-        if ((i & 63) == 63) {
-            if (ld_acquire_gpu(err) != 0) return false;
-            __nanosleep(100);
-        }
-    }
-    atomicExch(err, 1);
-    return false;
-}
-
 // D3Q19
 cudaError_t launch_d3q19_fused(const D3Args &a, int mode, bool mom, bool plot, cudaStream_t s);
 // native mode with storage kind (0 f32, 1 f16, 2 bf16) and optional Shan-Chen
@@ -170,14 +141,6 @@ cudaError_t launch_d2q9_fused(const D2Args &a, int mode, bool mom, bool plot, cu
 // launch_d2q9_fused without Shan-Chen or plot, as a programmatic dependent
 // launch (the grid may start while the previous kernel on s drains)
 cudaError_t launch_d2q9_fused_pdl(const D2Args &a, int mode, bool mom, cudaStream_t s);
-// every step of a batch in one cooperative launch (small lattices, no
-// Shan-Chen); sync holds a.H + 1 zeroed ints, sync[0] != 0 afterwards means a
-// block gave up waiting for a neighbour band.  cudaErrorCooperativeLaunchTooLarge
-// when the bands cannot all be resident.
-cudaError_t launch_d2q9_persistent(const D2Args &a, int mode, int nsteps, int *sync,
-                                   cudaStream_t s);
-// self-check of the persistent loop's bounded wait (sync: 2 zeroed ints)
-cudaError_t launch_band_wait_selftest(int *sync, int limit, cudaStream_t s);
 // temporal blocking (native mode, no Shan-Chen): one programmatic dependent
 // launch advances tblock_steps(variant) steps from a.src to a.dst; mom writes
 // the moments of the last one.  tblock_steps is 0 for an unknown variant.
@@ -225,7 +188,6 @@ struct ClosureArgs {
     float nu0, tau0, s_ref, z_max;
     float *y_out;     // optional: network output per cell (tests)
     int *err;         // device error word (tcgen05 kernel: an MMA that never completed)
-    int legacy_mma;   // 1: the warp-level mma.sync kernel instead of tcgen05
 };
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s);

@@ -130,14 +130,12 @@ __global__ void __launch_bounds__(128) tc05_wait_selftest_kernel(int *status, in
 }  // namespace lb
 
 extern "C" int lb_wait_selftest(int which, int *status_host) {
-    if (!status_host || which < 0 || which > 2) return LB_ERR_ARG;
+    if (!status_host || which < 1 || which > 2) return LB_ERR_ARG;
     int *dev = nullptr;
     cudaError_t e = cudaMalloc(&dev, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(dev, 0, 2 * sizeof(int));
     if (e == cudaSuccess) {
-        if (which == 0) {
-            e = lb::launch_band_wait_selftest(dev, 1 << 14, 0);
-        } else if (which == 2) {
+        if (which == 2) {
             e = lb::sc_stage_wait_selftest(dev);
         } else {
             lb::tc05_wait_selftest_kernel<<<1, 128>>>(dev, 1 << 10);

@@ -4,7 +4,9 @@ The closure network 19 -> 64 -> 64 -> 1 (ReLU), its mean-squared-error
 gradient, the Favre box filter of a fine lattice and the features / targets
 built from the filtered fields -- computed in float64 with the GPU kernels'
 rounding points (inputs, W1, W2 and the first hidden layer rounded to
-bfloat16).  Used only by the tests, to verify lb_closure.cu against.
+bfloat16 in the forward pass; the operands of the gradient contractions
+rounded to bfloat16 in the backward pass).  Used only by the tests, to
+verify lb_closure.cu against.
 """
 import numpy as np
 
@@ -50,26 +52,32 @@ def forward(p, X):
     return {"xb": xb, "h1": h1, "h2": h2, "y": y, "W2b": W2b}
 
 
-def grad(p, X, Z):
+def grad(p, X, Z, backward_bf16=True):
     """Gradient of mean((y - z)^2) over the rows, with the rounding treated as
     the identity in the backward pass except where the GPU backward rounds:
-    its contractions run on the tensor cores, so dH2 enters dH1 = dH2 W2 and
-    dW2 = dH2^T H1, and dH1 enters dW1 = dH1^T X, as bfloat16 (the bias
-    gradients sum the unrounded values)."""
+    every contraction over the samples runs on the tensor cores, so dH2
+    enters dH1 = dH2 W2, dW2 = dH2^T H1 and db2 = dH2^T 1, dH1 enters
+    dW1 = dH1^T X and db1 = dH1^T 1, and h2 and dy enter dw3 = H2^T dy and
+    db3 = dy^T 1, as bfloat16 (lb_closure.cu, mlp_tc_kernel).  With
+    backward_bf16=False the backward pass rounds nothing: the exact gradient
+    of the forward pass for the parameters behind its last rounding point."""
+    rb = bf16 if backward_bf16 else (lambda a: np.asarray(a, np.float64))
     W1, b1, W2, b2, w3, b3 = unpack(p)
     f = forward(p, X)
     n = len(X)
     dy = 2.0 * (f["y"] - Z) / n
+    dyb = rb(dy).astype(np.float64)
     g = np.zeros(NPARAM)
-    g[OFF_W3:OFF_B3] = f["h2"].T @ dy
-    g[OFF_B3] = dy.sum()
+    g[OFF_W3:OFF_B3] = rb(f["h2"]).astype(np.float64).T @ dyb
+    g[OFF_B3] = dyb.sum()
     dh2 = (dy[:, None] * w3[None, :]) * (f["h2"] > 0)
-    dh2b = bf16(dh2).astype(np.float64)
+    dh2b = rb(dh2).astype(np.float64)
     g[OFF_W2:OFF_B2] = (dh2b.T @ f["h1"]).reshape(-1)
-    g[OFF_B2:OFF_W3] = dh2.sum(0)
+    g[OFF_B2:OFF_W3] = dh2b.sum(0)
     dh1 = (dh2b @ f["W2b"]) * (f["h1"] > 0)
-    g[OFF_W1:OFF_B1] = (bf16(dh1).astype(np.float64).T @ f["xb"]).reshape(-1)
-    g[OFF_B1:OFF_W2] = dh1.sum(0)
+    dh1b = rb(dh1).astype(np.float64)
+    g[OFF_W1:OFF_B1] = (dh1b.T @ f["xb"]).reshape(-1)
+    g[OFF_B1:OFF_W2] = dh1b.sum(0)
     loss = float(np.mean((f["y"] - Z) ** 2))
     return g, loss
 

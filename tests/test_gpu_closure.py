@@ -178,38 +178,3 @@ def test_closure_speedup_at_equal_error(pkg):
     assert np.isfinite(runs["closure", 32]["ke_error"]) and runs["closure", 32]["ke_error"] < 0.1
     assert max(p["speedup"] or 0 for p in pairs) >= 1.5
 
-
-def test_closure_tcgen05_kernel_matches_warp_mma_kernel(pkg, oracle):
-    """The tensor-memory (tcgen05) closure kernel and the warp-level mma.sync
-    kernel evaluate the same network on the same BF16 operands; only the FP32
-    summation order inside the MMAs differs."""
-    C = pkg.closure
-    n = 32
-    N = n ** 3
-    net = C.Mlp(seed=5)
-    nu0, s_ref = 0.003, 0.05 * 2 * np.pi / n
-    rng = np.random.default_rng(8)
-    rho, ux, uy, uz = C.tgv_fields(n, 0.05)
-    ux = (ux + 0.01 * rng.standard_normal(N)).astype(np.float32)
-    f0 = oracle.d3q19_equilibrium(rho, ux, uy, uz, *pkg.W3)
-    f0 = (f0 * (1 + 0.002 * rng.standard_normal(f0.shape))).astype(np.float32)
-    L = pkg.lib()
-    outs = []
-    for tuning in (0x100, 0x110):  # tcgen05, then mma.sync
-        lat = pkg.Lattice(19, n, n, n, tau_inv=1.0, tuning=tuning)
-        lat.set_flags(np.zeros(N, np.uint8))
-        lat.set_populations(f0)
-        yd = C.DeviceArray(N)
-        assert L.lb_closure_enable(lat.h, net.h, np.float32(nu0), np.float32(s_ref),
-                                   np.float32(50.0), yd.ptr) == 0
-        lat.step(3)
-        lat.synchronize()
-        outs.append((yd.download(), lat.populations()))
-        lat.close()
-    (y_tc, f_tc), (y_mma, f_mma) = outs
-    assert np.isfinite(y_tc).all()
-    scale = np.abs(y_mma).max()
-    rel = np.abs(y_tc - y_mma) / scale
-    assert np.median(rel) < 1e-5 and rel.max() < 1e-2
-    np.testing.assert_allclose(f_tc, f_mma, rtol=1e-5, atol=1e-7)
-    net.close()

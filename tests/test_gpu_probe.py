@@ -70,8 +70,6 @@ CASES = {
                                                           rho_ref=0.693), (31, 15, 11), 11),
     "d3q19_shan_chen_staged_f32": (19, (64, 8, 8), dict(tau_inv=1.0, G=-5.0), (5, 3, 2), 13),
     "d2q9_pdl": (9, (72, 40, 1), dict(tau_inv=1.6, wall_u=(0.1, 0, 0)), (30, 1, 0), 70),
-    "d2q9_persistent": (9, (72, 40, 1), dict(tau_inv=1.6, wall_u=(0.1, 0, 0), tuning=0x104),
-                        (30, 1, 0), 70),
     "d2q9_shan_chen": (9, (48, 32, 1), dict(tau_inv=1.0, G=-5.0), (10, 11, 0), 17),
 }
 

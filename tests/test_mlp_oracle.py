@@ -1,7 +1,8 @@
 """CPU checks of the closure network's numpy oracle: its analytic gradient
 agrees with central finite differences for the parameters behind the last
-rounding point (b2, w3, b3, where the loss is smooth), and the filter/feature
-restatement recovers a known linear shear."""
+rounding point (b2, w3, b3, where the loss is smooth), the gradient with the
+GPU's bfloat16 backward operands stays within bfloat16 rounding of the exact
+one, and the filter/feature restatement recovers a known linear shear."""
 import sys
 
 import numpy as np
@@ -17,7 +18,7 @@ def test_gradient_vs_finite_differences():
     p = rng.standard_normal(M.NPARAM) * 0.3
     X = rng.standard_normal((64, 19)).astype(np.float32)
     Z = rng.standard_normal(64)
-    g, _ = M.grad(p, X, Z)
+    g, _ = M.grad(p, X, Z, backward_bf16=False)
     for idx in list(range(M.OFF_B2, M.OFF_B2 + 8)) + list(range(M.OFF_W3, M.OFF_W3 + 8)) + \
             [M.OFF_B3]:
         e = 1e-6
@@ -27,6 +28,22 @@ def test_gradient_vs_finite_differences():
         q[idx] -= 2 * e
         lm = M.grad(q, X, Z)[1]
         assert abs(g[idx] - (lp - lm) / (2 * e)) <= 1e-6 + 1e-5 * abs(g[idx])
+
+
+def test_bf16_backward_operands_stay_near_the_exact_gradient():
+    """Rounding the gradient contractions' operands to bfloat16 (8 significant
+    bits) moves each parameter group by a few parts in 10^3."""
+    rng = np.random.default_rng(3)
+    p = rng.standard_normal(M.NPARAM) * 0.3
+    X = rng.standard_normal((512, 19)).astype(np.float32)
+    Z = rng.standard_normal(512)
+    g, loss = M.grad(p, X, Z)
+    e, loss_e = M.grad(p, X, Z, backward_bf16=False)
+    assert loss == loss_e
+    for a, b in [(M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2),
+                 (M.OFF_B2, M.OFF_W3), (M.OFF_W3, M.OFF_B3)]:
+        assert np.linalg.norm(g[a:b] - e[a:b]) <= 4e-3 * np.linalg.norm(e[a:b])
+    assert abs(g[M.OFF_B3] - e[M.OFF_B3]) <= 4e-3 * np.abs(e[M.OFF_B3])
 
 
 def test_features_of_uniform_shear():
