@@ -766,7 +766,8 @@ def measure_e2e_dropin(pkg, L, wl, flags, steps, fused=True):
     per step, streaming_d3q19, collision_d3q19 into the plot buffer (Zou-He
     velocity inlet u = 0 at x = 0 and pressure outlet rho = 1 at x = nx-1,
     full-way bounce-back walls and sphere), read_value_3d at the cursor and a
-    16-byte device-to-host copy, as SimulationD3Q19::runLBM does
+    16-byte device-to-host copy (queued in stream order), as
+    SimulationD3Q19::runLBM does
     (src/simulation_d3q19.cu:350-430).  tau = 0.8: at 0.55 the reference's
     own Zou-He faces grow a disturbance on this geometry (the oracle, the
     reference compiled for the host, does the same).  Timed with host
@@ -821,7 +822,8 @@ def measure_e2e_dropin(pkg, L, wl, flags, steps, fused=True):
             "h2d_bytes_per_step": 4 * 19 * N / steps, "d2h_bytes_per_step": (16 * steps + 16 * N) / steps,
             "mode": "fused" if fused else "standalone",
             "path": "lb_run_lbm_d3q19: per step streaming_d3q19 + collision_d3q19 (plot buffer) "
-                    "+ read_value_3d + a 16-byte synchronous copy to pinned host memory; the "
+                    "+ read_value_3d + a 16-byte copy to pinned host memory in stream order "
+                    "(one host wait after the last step); the "
                     "reference's semantics (Zou-He x faces, full-way bounce-back), tau 0.8",
             "bytes_per_lu": 185 if fused else 330}
 

@@ -115,9 +115,11 @@ int lb_reduce_d3q19_noalloc(const DataD3Q19 *data, double out[7]);
 /* The reference's per-step host sequence (SimulationD3Q19::runLBM, reference
  * src/simulation_d3q19.cu:350-430, without the GL map/unmap and the extra
  * device-wide synchronisations): for each step streaming_d3q19,
- * collision_d3q19 into plot_data, read_value_3d at the cursor and a 16-byte
- * device-to-host copy of data->valueCur into value_host[4] (the value of the
- * last step is left there).  Returns LB_OK or LB_ERR_CUDA (message in
+ * collision_d3q19 into plot_data, read_value_3d's kernel at the cursor and
+ * a 16-byte device-to-host copy of data->valueCur into value_host[4], all
+ * queued in stream order (the host waits once, after the last step; the
+ * value of the last step is left in value_host).  Returns LB_OK, LB_ERR_ARG
+ * (bad struct or cursor outside the lattice) or LB_ERR_CUDA (message in
  * lb_abi_last_error). */
 typedef struct {
     float w0, w1, w7, tau_inv, ux_in, uy_in, uz_in, rho_out;

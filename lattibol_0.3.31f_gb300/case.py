@@ -246,6 +246,7 @@ class _Simulation:
         L = _lib()
         self.output.updateSteps = n
         L.lb_device_synchronize()
+        L.lb_abi_clear_error()  # report only what this run's entry points record
         t0 = time.perf_counter()
         for _ in range(n):
             self._step(L)

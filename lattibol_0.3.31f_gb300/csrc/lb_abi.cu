@@ -154,11 +154,15 @@ void streaming_d3q19(DataD3Q19 *data, dim3, dim3) {
     if (e != cudaSuccess) set_err("streaming_d3q19", e);
 }
 
-void collision_d3q19(float *plot_data, DataD3Q19 *data, float w0, float w1, float w7,
-                     float tau_inv, float ux_in, float uy_in, float uz_in, float rho_out,
-                     float u_min, float u_max, float rho_min, float rho_max, dim3, dim3) {
-    (void)uy_in; (void)uz_in; (void)u_min; (void)u_max; (void)rho_min; (void)rho_max;
-    if (bad_d3(data, "collision_d3q19")) return;
+}  // extern "C"
+
+namespace {
+// collision_d3q19's work.  In fused mode a non-null probe (device-accessible,
+// 16-byte aligned) receives the (ux, uy, uz, rho) that the pass writes into
+// the plot buffer at node probe_o.  Returns true when the fused pass ran.
+bool collide_d3q19(float *plot_data, DataD3Q19 *data, float w0, float w1, float w7,
+                   float tau_inv, float ux_in, float rho_out, float4 *probe, int probe_o) {
+    if (bad_d3(data, "collision_d3q19")) return false;
     std::lock_guard<std::mutex> l(g_mu);
     D3Args a = d3_args(data);
     a.w0 = w0; a.w1 = w1; a.w7 = w7; a.tau_inv = tau_inv; a.ux_in = ux_in; a.rho_out = rho_out;
@@ -172,16 +176,29 @@ void collision_d3q19(float *plot_data, DataD3Q19 *data, float w0, float w1, floa
         float *const *dst = ours ? s.orig : s.lib;
         a.src = cpop_of<19>(cur);
         a.dst = pop_of<19>(dst);
+        a.probe = probe;
+        a.probe_o = probe_o;
         cudaError_t e = launch_d3q19_fused(a, MODE_REF, true, plot_data != nullptr, 0);
         s.pending = false;
-        if (e != cudaSuccess) { set_err("collision_d3q19", e); return; }
+        if (e != cudaSuccess) { set_err("collision_d3q19", e); return false; }
         for (int k = 0; k < 19; k++) cur[k] = dst[k];
-        return;
+        return true;
     }
     a.src = cpop_of<19>(cur);
     a.dst = pop_of<19>(cur);
     cudaError_t e = launch_d3q19_collide(a, plot_data != nullptr, 0);
     if (e != cudaSuccess) set_err("collision_d3q19", e);
+    return false;
+}
+}  // namespace
+
+extern "C" {
+
+void collision_d3q19(float *plot_data, DataD3Q19 *data, float w0, float w1, float w7,
+                     float tau_inv, float ux_in, float uy_in, float uz_in, float rho_out,
+                     float u_min, float u_max, float rho_min, float rho_max, dim3, dim3) {
+    (void)uy_in; (void)uz_in; (void)u_min; (void)u_max; (void)rho_min; (void)rho_max;
+    collide_d3q19(plot_data, data, w0, w1, w7, tau_inv, ux_in, rho_out, nullptr, 0);
 }
 
 void get_border_d3q19(DataD3Q19 *data, dim3, dim3) {
@@ -348,16 +365,50 @@ int lb_run_lbm_d3q19(DataD3Q19 *data, float *plot_data, const lb_run_params_d3q1
     if (!data || !p || !value_host || steps < 0) return LB_ERR_ARG;
     const dim3 g(1, 1, 1), b(32, 4, 1);  // accepted and ignored, as by every entry point
     g_err.clear();
+    if (bad_d3(data, "lb_run_lbm_d3q19")) return LB_ERR_ARG;
+    const int cx = p->cursor[0], cy = p->cursor[1], cz = p->cursor[2];
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= data->width || cy >= data->height ||
+        cz >= data->depth) {
+        set_err("lb_run_lbm_d3q19", "cursor outside the lattice");
+        return LB_ERR_ARG;
+    }
+    const long o = cx + (long)cy * data->width + (long)cz * data->width * data->height;
+    // Each step's cursor value goes to value_host in stream order behind the
+    // step, without read_value_3d's device-wide synchronisation, and the host
+    // waits once, after the last step (as the per-step synchronous sequence
+    // did, value_host then holds the last step's value):
+    //  * page-locked, mapped value_host and the fused pass: the pass writes
+    //    the cursor's plot value into it directly (its probe), and
+    //    data->valueCur is filled once after the last step;
+    //  * otherwise read_value_3d's kernel and a 16-byte copy per step.
+    float4 *probe = nullptr;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, value_host) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        reinterpret_cast<uintptr_t>(pa.devicePointer) % 16 == 0 && o < (1L << 31))
+        probe = reinterpret_cast<float4 *>(pa.devicePointer);
+    else
+        (void)cudaGetLastError();
+    bool probed = false;  // the last step's value went to value_host through the probe
     for (int i = 0; i < steps; i++) {
         streaming_d3q19(data, g, b);
-        collision_d3q19(plot_data, data, p->w0, p->w1, p->w7, p->tau_inv, p->ux_in, p->uy_in,
-                        p->uz_in, p->rho_out, 0.f, 0.f, 0.f, 0.f, g, b);
-        read_value_3d(plot_data, data, p->cursor[0], p->cursor[1], p->cursor[2]);
+        probed = collide_d3q19(plot_data, data, p->w0, p->w1, p->w7, p->tau_inv, p->ux_in,
+                               p->rho_out, probe, (int)o) &&
+                 probe && plot_data;
         if (!g_err.empty()) return LB_ERR_CUDA;
-        cudaError_t e = cudaMemcpy(value_host, data->valueCur, 4 * sizeof(float),
-                                   cudaMemcpyDeviceToHost);
+        if (probed) continue;
+        cudaError_t e = launch_read_value(plot_data, data->ux, data->uy, data->uz, data->rho,
+                                          data->valueCur, o, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(value_host, data->valueCur, 4 * sizeof(float),
+                                cudaMemcpyDeviceToHost, 0);
         if (e != cudaSuccess) { set_err("lb_run_lbm_d3q19", e); return LB_ERR_CUDA; }
     }
+    cudaError_t e = probed ? launch_read_value(plot_data, data->ux, data->uy, data->uz,
+                                               data->rho, data->valueCur, o, 0)
+                           : cudaSuccess;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) { set_err("lb_run_lbm_d3q19", e); return LB_ERR_CUDA; }
     return LB_OK;
 }
 
