@@ -302,9 +302,12 @@ int64_t lb_ensemble_launch_count(const lb_ensemble *e);
 /* A 19 -> 64 -> 64 -> 1 ReLU network maps each cell's non-equilibrium
  * moments and |S| to an eddy viscosity nu_t = nu0 * clamp(y, 0, z_max); the
  * closure kernel relaxes the cell with tau = 0.5 + 3 (nu0 + nu_t).  The
- * network runs on the tensor cores (BF16 weights and activations, FP32
- * accumulate) inside the collision kernel; training uses the same forward
- * pass, an FP32 backward pass and Adam, all on the GPU. */
+ * network runs on the tcgen05 tensor cores (BF16 weights and activations,
+ * FP32 accumulators in tensor memory) inside the collision kernel; training
+ * runs its forward and backward passes on the tensor cores the same way
+ * (the gradient contractions' operands in BF16, FP32 accumulation) and Adam,
+ * all on the GPU.  Every tensor-core wait is bounded: a network call whose
+ * MMA never completed returns LB_ERR_CUDA (lb_mlp_error says so). */
 typedef struct lb_mlp lb_mlp;
 int lb_mlp_create(uint64_t seed, lb_mlp **out);  /* He-uniform initial weights */
 int lb_mlp_destroy(lb_mlp *m);
