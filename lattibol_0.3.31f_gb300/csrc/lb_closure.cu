@@ -122,6 +122,16 @@ __device__ __forceinline__ uint32_t bf16x2_relu(float lo, float hi) {
     return d;
 }
 
+// n / d for 32-bit n and d by one multiply-high with c = floor((2^64 - 1) / d)
+// + 1 (exact for every 32-bit n and d >= 2: Lemire, Kaser and Kurz, "Faster
+// remainder by direct computation", 2019); d = 1 is n itself
+__host__ __device__ __forceinline__ uint64_t div_constant(uint32_t d) {
+    return d > 1 ? ~0ull / d + 1 : 0;
+}
+__device__ __forceinline__ uint32_t div_u32(uint32_t n, uint64_t c, uint32_t d) {
+    return d > 1 ? (uint32_t)__umul64hi(c, (uint64_t)n) : n;
+}
+
 constexpr int TC_COLS = 64;             // tensor-memory columns per block (D is 128 x 64)
 constexpr int TC_WAIT = 1 << 22;        // mbarrier polls before a block gives up
 
@@ -173,8 +183,8 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         const int oo = rr * D3_BLOCK + t;
         u.inside = oo < ncell;
         u.o = u.inside ? oo : 0;
-        const int z = u.o / WH, rem = u.o - z * WH;
-        const int y = rem / a.W, x = rem - y * a.W;
+        const int z = (int)div_u32((uint32_t)u.o, ca.div_wh, (uint32_t)WH), rem = u.o - z * WH;
+        const int y = (int)div_u32((uint32_t)rem, ca.div_w, (uint32_t)a.W), x = rem - y * a.W;
         const uint8_t fl = u.inside ? a.flags[u.o] : CELL_WALL;
         u.fluid = !(fl & CELL_WALL);
         if (u.fluid) {
@@ -340,8 +350,11 @@ cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mo
     }
     const long nrows = ((long)a.W * a.H * a.D + D3_BLOCK - 1) / D3_BLOCK;
     const unsigned g = (unsigned)(nrows < tc_cap ? nrows : tc_cap);
-    if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, ca);
-    else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, ca);
+    ClosureArgs c = ca;
+    c.div_wh = div_constant((uint32_t)(a.W * a.H));
+    c.div_w = div_constant((uint32_t)a.W);
+    if (mom) d3q19_closure_tc_kernel<true><<<g, D3_BLOCK, 0, s>>>(a, c);
+    else d3q19_closure_tc_kernel<false><<<g, D3_BLOCK, 0, s>>>(a, c);
     return cudaGetLastError();
 }
 

@@ -188,6 +188,8 @@ struct ClosureArgs {
     float nu0, tau0, s_ref, z_max;
     float *y_out;     // optional: network output per cell (tests)
     int *err;         // device error word (tcgen05 kernel: an MMA that never completed)
+    // division by W*H and by W as a multiply-high (set by launch_d3q19_closure)
+    uint64_t div_wh, div_w;
 };
 cudaError_t launch_d3q19_closure(const D3Args &a, const ClosureArgs &ca, bool mom,
                                  cudaStream_t s);
