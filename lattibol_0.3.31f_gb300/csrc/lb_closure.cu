@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(D3_BLOCK) d3q19_closure_tc_kernel(const D3Args
         u.fluid = !(fl & CELL_WALL);
         if (u.fluid) {
             const Nbr3 n(x, y, z, a.W, a.H, a.D);
-            pull_native<float>(a, u.o, n, fl, u.g);
+            pull_native<float, true>(a, u.o, n, fl, u.g);
         }
     };
     // The next run's populations are loaded while this run's network runs on

@@ -39,8 +39,10 @@ struct Coord3 {
 };
 
 // Native pull of the 19 populations of fluid node o (see d3q19_fused_kernel):
-// f_k in FP32 storage, the deviation d_k in 16-bit storage.
-template <typename S>
+// f_k in FP32 storage, the deviation d_k in 16-bit storage.  IDX32: each
+// upstream index is summed in 32 bits before the one pointer addition (fewer
+// instructions, a few more registers; for the issue-bound closure kernel).
+template <typename S, bool IDX32 = false>
 __device__ __forceinline__ void pull_native(const D3Args &a, int o, const Nbr3 &n, uint8_t fl,
                                             float (&g)[19]) {
     const S *const *src = (const S *const *)(a.src.f);  // storage arrays behind float*
@@ -58,8 +60,12 @@ __device__ __forceinline__ void pull_native(const D3Args &a, int o, const Nbr3 &
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < 19; k++)
-            g[k] = Store<S>::load_dev(src[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)));
+        for (int k = 0; k < 19; k++) {
+            if (IDX32)
+                g[k] = Store<S>::load_dev(src[k] + (o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k))));
+            else
+                g[k] = Store<S>::load_dev(src[k] + o + n.off(-d3_cx(k), -d3_cy(k), -d3_cz(k)));
+        }
     }
 }
 
