@@ -25,10 +25,14 @@ def pkg():
     return p
 
 
-def test_mlp_forward_matches_oracle(pkg):
+# 100 003 samples: more 128-sample tiles than the launches have blocks, so
+# blocks take several tiles (the training kernel's gradient sums accumulate
+# in tensor memory across them) and the last tile is ragged
+@pytest.mark.parametrize("n", [1000, 100003])
+def test_mlp_forward_matches_oracle(pkg, n):
     net = pkg.closure.Mlp(seed=3)
     rng = np.random.default_rng(0)
-    X = rng.standard_normal((1000, 19)).astype(np.float32)
+    X = rng.standard_normal((n, 19)).astype(np.float32)
     y = net.forward(X)
     ref = mlp_oracle.forward(net.params(), X)["y"]
     # FP32 accumulation order only (identical bf16 rounding points)
@@ -36,11 +40,12 @@ def test_mlp_forward_matches_oracle(pkg):
     net.close()
 
 
-def test_mlp_gradient_matches_oracle(pkg):
+@pytest.mark.parametrize("n", [777, 100003])  # neither a multiple of 128
+def test_mlp_gradient_matches_oracle(pkg, n):
     net = pkg.closure.Mlp(seed=5)
     rng = np.random.default_rng(1)
-    X = rng.standard_normal((777, 19)).astype(np.float32)  # not a multiple of 128
-    Z = rng.standard_normal(777).astype(np.float32)
+    X = rng.standard_normal((n, 19)).astype(np.float32)
+    Z = rng.standard_normal(n).astype(np.float32)
     g, loss = net.grad(X, Z)
     g_ref, loss_ref = mlp_oracle.grad(net.params(), X, Z)
     assert abs(loss - loss_ref) <= 1e-4 * abs(loss_ref)
