@@ -117,11 +117,22 @@ __global__ void __launch_bounds__(NT) d2q9_tblock_kernel(const D2Args a) {
     const int W = a.W, H = a.H;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     if (threadIdx.x < 9) corr[threadIdx.x] = a.corr[threadIdx.x];
-    // region node (rx, ry) is lattice node (x0 - TS + rx, y0 - TS + ry), wrapped
+    // region node (rx, ry) is lattice node (x0 - TS + rx, y0 - TS + ry),
+    // wrapped: one conditional add or subtract when the lattice is at least a
+    // tile and its halo wide and high (every coordinate then lies within one
+    // period of the lattice), the remainder otherwise
+    const bool one_wrap = W >= BX + TS && H >= BY + TS;
     for (int i = threadIdx.x; i < RN; i += NT) {
-        int gx = (x0 - TS + i % RX) % W, gy = (y0 - TS + i / RX) % H;
-        gx += gx < 0 ? W : 0;
-        gy += gy < 0 ? H : 0;
+        int gx = x0 - TS + i % RX, gy = y0 - TS + i / RX;
+        if (one_wrap) {
+            gx = gx < 0 ? gx + W : (gx >= W ? gx - W : gx);
+            gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+        } else {
+            gx %= W;
+            gy %= H;
+            gx += gx < 0 ? W : 0;
+            gy += gy < 0 ? H : 0;
+        }
         const int o = gx + W * gy;
         fl[i] = a.flags[o];
 #pragma unroll
