@@ -432,8 +432,13 @@ int lb_create(const lb_config *cfg, lb_ctx **out) {
     if (c->cfg.graph_steps <= 0) c->cfg.graph_steps = 64;
     c->cfg.graph_steps += c->cfg.graph_steps & 1;  // even: a graph returns to its start set
     if (!(c->cfg.rho_ref > 0.f)) c->cfg.rho_ref = 1.f;
+    // explicit: the bits the header defines (REVERSE, PDL, TBLOCK, SC_STAGED,
+    // SC_NO_TMA, the block shape); any other bit is ignored
+    constexpr int kTuneBits = LB_TUNE_REVERSE | LB_TUNE_PDL | LB_TUNE_TBLOCK | LB_TUNE_SC_STAGED |
+                              LB_TUNE_SC_NO_TMA | LB_TUNE_TBLOCK_SHAPE(0x1f);
+    static_assert(kTuneBits == 0x1f0e9, "tuning bits");
     c->tune = (cfg->tuning & LB_TUNE_EXPLICIT)
-                  ? (cfg->tuning & 0x1f0eb)
+                  ? (cfg->tuning & kTuneBits)
                   : (cfg->lattice == LB_D2Q9 ? LB_TUNE_LIBRARY_DEFAULT_D2
                                              : LB_TUNE_LIBRARY_DEFAULT_D3);
     if (!(cfg->tuning & LB_TUNE_EXPLICIT) && cfg->lattice == LB_D2Q9 &&
