@@ -40,11 +40,11 @@ class Workload:
     algorithmic bytes per lattice update of the kernel it times."""
 
     def __init__(self, name, lattice, size, tau, steps, bytes_per_lu, force=(0, 0, 0),
-                 wall_u=(0, 0, 0), traffic=None, profile=None, describe=None, G=0.0,
+                 wall_u=(0, 0, 0), traffic=None, describe=None, G=0.0,
                  storage=0, rho_ref=0.0, dtype="f32"):
         self.name, self.lattice, self.size, self.tau = name, lattice, tuple(size), tau
         self.steps, self.bytes_per_lu, self.force, self.wall_u = steps, bytes_per_lu, force, wall_u
-        self.traffic, self.profile, self.describe = traffic, profile, describe or {}
+        self.traffic, self.describe = traffic, describe or {}
         self.G, self.storage, self.rho_ref, self.dtype = G, storage, rho_ref, dtype
 
     def initial_rho(self):
@@ -90,11 +90,11 @@ WORKLOADS = {
     # 19x4 loads + 19x4 stores + 1 flag byte (moments only on the last step)
     "channel": Workload(
         "channel", 19, (256, 128, 128), 0.55, 20000, 2 * 19 * 4 + 1, force=(1e-6, 0, 0),
-        # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum),
-        # captured on this lattice with the caches left as the previous step
-        # left them (ncu --cache-control none, mean of two launches; the
-        # capture is in profiles/d3q19_fused_channel_256x128x128.md)
-        traffic=578.4e6, profile="profiles/d3q19_fused_channel_256x128x128.md",
+        # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+        # of d3q19_fused_kernel, captured on this lattice with the caches left
+        # as the previous step left them (ncu --cache-control none, mean of
+        # two launches)
+        traffic=578.4e6,
         describe={"body_force_x": 1e-6, "sphere": {"center": [64, 64, 64], "radius": 16},
                   "boundaries": "x periodic, half-way bounce-back on y/z faces and sphere",
                   "init": "equilibrium rho=1 u=0",
